@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Benchmark: 3-D Richardson-Lucy deconvolution in FP32 on one GB300.
+
+Workload (the 3-D RL configuration): a 256x256x64 volume of 200 ellipsoids (radii 2-20,
+intensities 50-1000) on background 10, blurred by a normalised anisotropic Gaussian PSF
+15x15x7 (sigma 2, 2, 1) with Poisson noise; flat start at the mean; 50 iterations of
+non-separable direct convolution, zero border. One step = one complete 50-iteration run
+(100 fused convolution passes). Data are synthetic and seeded.
+
+Metric: convolution throughput in GVoxel/s = output voxels of all convolutions in the
+step (2 per iteration) / time. `value` is device time (CUDA events) with inputs resident
+in HBM and L2 flushed (a 256 MB write) before every step; `e2e` is the same metric through
+the C-ABI host entry point (pinned host observed image in, host estimate out, both copies
+inside the timed region).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+N > 1 runs under torchrun as independent replicas (the RL volume does not shard); the
+reference arm times the reference's CPU implementation (the oracle port, all host threads)
+on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SHAPE_XYZ = (256, 256, 64)
+PSF_XYZ = (15, 15, 7)
+ITERATIONS = 50
+EPSILON = 1e-6
+VOXELS = SHAPE_XYZ[0] * SHAPE_XYZ[1] * SHAPE_XYZ[2]
+TAPS = PSF_XYZ[0] * PSF_XYZ[1] * PSF_XYZ[2]
+METRIC = "Conv GVoxel/s (3-D RL FP32, fused passes)"
+UNIT = "GVoxel/s"
+WORKLOAD = "rl3d_f32_256x256x64_psf15x15x7_50it"
+SLAB_PLANES = 16  # CPU sample: two full-width convolutions over a 16-plane slab
+
+
+def config(extra=None):
+    c = {
+        "workload": WORKLOAD,
+        "volume_xyz": list(SHAPE_XYZ),
+        "psf_xyz": list(PSF_XYZ),
+        "psf_sigma_xyz": [2.0, 2.0, 1.0],
+        "iterations": ITERATIONS,
+        "init": "flat start at mean",
+        "border": "zero",
+        "l2": "flushed before every timed step (256 MB write)",
+        "parallelism": "replicas",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "", 1).isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()), "measured"
+        except ValueError:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def recorded_traffic():
+    """Per-launch DRAM bytes of the fused pass from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get(WORKLOAD)
+        except ValueError:
+            return None
+    return None
+
+
+def cpu_sample(observed, psf, threads):
+    """Two convolutions (one RL iteration's convolution work) over a slab, on the oracle."""
+    import numpy as np
+
+    import oracle
+
+    slab = np.ascontiguousarray(observed[:SLAB_PLANES])
+    tmp = np.empty_like(slab)
+    adj = np.ascontiguousarray(psf[::-1, ::-1, ::-1])
+    t0 = time.perf_counter()
+    oracle.convolve(slab, psf, tmp, "zero", threads=threads)
+    oracle.convolve(tmp, adj, slab.copy(), "zero", threads=threads)
+    dt = time.perf_counter() - t0
+    return 2 * slab.size / dt / 1e9, dt
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference's CPU convolution path (the oracle port; the reference's
+    own build is not available on this host), all host threads, bounded slab samples."""
+    if rank != 0:
+        return
+    import numpy as np  # noqa: F401
+
+    from iane_gb300 import synth
+    from oracle import build as oracle_build
+
+    import oracle
+
+    oracle_build.build_oracle()
+    threads = oracle.default_threads()
+    observed, psf, _ = synth.rl_volume_workload(seed=0)
+    for _ in range(args.warmup):
+        cpu_sample(observed, psf, threads)
+    total = 0.0
+    for _ in range(args.steps):
+        _, dt = cpu_sample(observed, psf, threads)
+        total += dt
+    voxels = 2 * SLAB_PLANES * SHAPE_XYZ[0] * SHAPE_XYZ[1]
+    value = voxels * args.steps / total / 1e9
+    sample = f"two zero-border 15x15x7 convolutions over a 256x256x{SLAB_PLANES} slab per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 accumulate",
+        "data": "synthetic", "config": config({"sample": sample}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    import iane_gb300
+    from iane_gb300 import synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    observed, psf, _ = synth.rl_volume_workload(seed=0)
+    obs_host = torch.from_numpy(observed).pin_memory()
+    est_host = torch.empty(observed.shape, dtype=torch.float32).pin_memory()
+    obs = obs_host.to(dev)
+    rl = iane_gb300.RichardsonLucy(torch.from_numpy(psf).to(dev), observed.shape)
+    scratch = torch.empty(rl.scratch_bytes, dtype=torch.uint8, device=dev)
+    host_scratch = torch.empty(rl.host_scratch_bytes(False), dtype=torch.uint8, device=dev)
+    est = torch.empty(observed.shape, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        rl.run(obs, est, ITERATIONS, EPSILON, init=rl.INIT_MEAN, scratch=scratch, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    events = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        events.append((a, b))
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    iane_gb300.device_status()
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    conv_voxels_per_step = 2 * ITERATIONS * VOXELS
+    value = world * conv_voxels_per_step * args.steps / (total_ms / 1e3) / 1e9
+    ms_per_step = total_ms / args.steps
+
+    # end to end through the C-ABI host entry point
+    e2e_steps = max(3, min(args.steps, 10))
+    rl.run_host(obs_host, est_host, ITERATIONS, EPSILON, init=rl.INIT_MEAN, scratch=host_scratch)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rl.run_host(obs_host, est_host, ITERATIONS, EPSILON, init=rl.INIT_MEAN, scratch=host_scratch)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * conv_voxels_per_step * e2e_steps / e2e_s / 1e9
+
+    # result sanity: the run converged to something finite and positive
+    est_np = est.cpu().numpy()
+    assert np.isfinite(est_np).all() and est_np.min() >= 0.0
+
+    # roofline of the fused pass (100 launches per step; the two init kernels are tiny,
+    # so step time / 100 bounds the average pass duration from above)
+    peaks, peak_kind = measured_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s at the maximum SM clock
+    pass_ms = ms_per_step / (2 * ITERATIONS)
+    flops_per_pass = 2.0 * TAPS * VOXELS
+    achieved = flops_per_pass / (pass_ms / 1e3) / 1e12
+    alg_bytes_pass = 12.0 * VOXELS
+    hbm_achieved = alg_bytes_pass / (pass_ms / 1e3) / 1e9
+    traffic = recorded_traffic()
+    roofline = {
+        "bound": "fp32",
+        "achieved": achieved,
+        "peak": fp32_peak,
+        "unit": "TFLOP/s",
+        "frac": achieved / fp32_peak,
+        "traffic": traffic,
+        "kernel": "conv_tile_kernel<15,2,2,TMA> (RL pass A/B)",
+        "peak_source": f"derived: 152 SMs x 128 FP32 FMA/clk x 2 x sm_max_mhz {sm_max:.0f} ({peak_kind} peaks file);"
+                       " no FP32-SIMT peak is measured, the kernel is FP32-pipe bound",
+        "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": float(peaks.get("hbm_gbs", 6800.0)),
+                "frac": hbm_achieved / float(peaks.get("hbm_gbs", 6800.0)), "alg_bytes_per_pass": alg_bytes_pass},
+        "frac_at_sampled_clock": (achieved / (152 * 256 * clocks["sm_mhz"] * 1e6 / 1e12)
+                                  if clocks.get("sm_mhz") else None),
+    }
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        from oracle import build as oracle_build
+
+        oracle_build.build_oracle()
+        threads = oracle.default_threads()
+        v, dt = cpu_sample(observed, psf, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"two zero-border 15x15x7 convolutions over a 256x256x{SLAB_PLANES} slab ({dt:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipsoid phantom, Poisson)",
+            "config": config(), "rl_iterations_per_s": world * ITERATIONS * args.steps / (total_ms / 1e3),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(observed.nbytes),
+                    "d2h_bytes_per_step": int(observed.nbytes), "steps": e2e_steps},
+            "gpu_launches": (2 + 2 * ITERATIONS) * args.steps,
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+        }
+        print(json.dumps(line), flush=True)
+    rl.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

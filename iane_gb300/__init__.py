@@ -1,0 +1,155 @@
+"""GB300-native IANE convolution and Richardson-Lucy deconvolution.
+
+Python mirror of the reference interface for this path, over torch CUDA tensors (torch
+supplies device memory and streams only; every computation runs in ``libiane_gb300.so``):
+
+* :func:`convolve` -- ``iane::convolve(src, kernel, dst, {border}, cuda_policy{stream})``
+  (reference include/iane/algorithms/convolution.hpp:97-117): odd kernel extents, the
+  kernel flipped, same extents in and out, reference casts for integer outputs.
+* :func:`convolve_separable` -- the same with an outer-product kernel, one fused pass.
+* :class:`RichardsonLucy` -- the prepared-algorithm protocol of
+  include/iane/execution/prepared.hpp:120-146 (``prepare`` sizes the scratch, ``run``
+  consumes it) applied to the RL loop of examples/rl_deconvolution/main.cu:51-81.
+
+Tensors are C-ordered (slowest axis first): a tensor of shape ``(nz, ny, nx)`` is the IANE
+view with extents ``[nx, ny, nz]``. Kernels are indexed the same way.
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import abi
+from ._lib import IaneError, IaneInvalidArgument, IaneLengthError, check, lib
+
+__all__ = [
+    "abi", "convolve", "convolve_separable", "RichardsonLucy", "device_status", "IaneError",
+    "IaneInvalidArgument", "IaneLengthError",
+]
+
+
+def _stream_handle(stream) -> int:
+    import torch
+
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream)
+
+
+def _border(border) -> int:
+    if isinstance(border, str):
+        if border not in abi.BORDERS:
+            raise ValueError(f"unknown border {border!r}")
+        return abi.BORDERS[border]
+    return int(border)
+
+
+def _device_view(t) -> abi.View:
+    if not t.is_cuda:
+        raise ValueError("iane_gb300 works on CUDA tensors; copy host data to the device first")
+    return abi.torch_view(t)
+
+
+def convolve(src, kernel, dst, border="clamp", exact: bool = False, stream=None):
+    """Direct convolution of ``src`` with ``kernel`` into ``dst`` (all CUDA tensors).
+
+    ``exact=True`` accumulates in FP64 in the reference's tap order, giving results
+    bit-identical to the reference's CPU convolution; the default is FP32 accumulation
+    (int64 for integer image/kernel pairs). Asynchronous on ``stream``."""
+    s, k, d = _device_view(src), _device_view(kernel), _device_view(dst)
+    flags = abi.ACC_EXACT if exact else abi.ACC_FAST
+    check(lib().iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), _border(border), flags,
+                                 _stream_handle(stream)))
+    return dst
+
+
+def convolve_separable(src, taps, dst, border="clamp", stream=None):
+    """Convolution with the outer product of 1-D f32 ``taps`` (``taps[i]`` for IANE axis i,
+    i.e. ``taps[0]`` runs along the last tensor dimension)."""
+    s, d = _device_view(src), _device_view(dst)
+    views = [_device_view(t) for t in taps]
+    arr = (ctypes.POINTER(abi.View) * max(1, len(views)))(*[ctypes.pointer(v) for v in views])
+    check(lib().iane_gb_convolve_separable(ctypes.byref(s), arr, ctypes.byref(d), _border(border),
+                                           _stream_handle(stream)))
+    return dst
+
+
+def device_status(stream=None) -> None:
+    """Raise if a bounded device-side wait of an earlier launch gave up."""
+    check(lib().iane_gb_device_status(_stream_handle(stream)))
+
+
+class RichardsonLucy:
+    """Prepared Richardson-Lucy deconvolution for one image shape and PSF.
+
+    ``prepare`` copies the PSF, builds its adjoint and the exact edge-sensitivity table
+    (the reference computes sensitivity = convolve(1, adjoint, zero border) per prepare,
+    examples/rl_deconvolution/main.cu:62-64). ``scratch_bytes`` is what ``run`` needs, as
+    in the reference's prepared protocol; ``run`` allocates it with torch when no scratch
+    tensor is passed.
+    """
+
+    INIT_OBSERVED = abi.RL_INIT_OBSERVED
+    INIT_MEAN = abi.RL_INIT_MEAN
+    INIT_GIVEN = abi.RL_INIT_GIVEN
+
+    def __init__(self, psf, shape, stream=None):
+        self.shape = tuple(int(s) for s in shape)
+        rank = len(self.shape)
+        ext = (ctypes.c_int32 * 3)(*([self.shape[rank - 1 - i] for i in range(rank)] + [1] * (3 - rank)))
+        handle = ctypes.c_void_p()
+        v = _device_view(psf)
+        check(lib().iane_gb_rl_prepare(ctypes.byref(v), rank, ext, _stream_handle(stream), ctypes.byref(handle)))
+        self._plan = handle
+        self.scratch_bytes = int(lib().iane_gb_rl_scratch_bytes(handle))
+
+    def host_scratch_bytes(self, observed_u8: bool = False) -> int:
+        return int(lib().iane_gb_rl_host_scratch_bytes(self._plan, abi.U8 if observed_u8 else abi.F32))
+
+    def run(self, observed, estimate, iterations: int, epsilon: float = 1e-6, init: int = abi.RL_INIT_OBSERVED,
+            scratch=None, stats=None, stream=None):
+        """Run ``iterations`` RL iterations; ``estimate`` receives the result (f32 or u8).
+
+        ``stats``: optional CUDA float64 tensor with ``2 * iterations`` entries receiving
+        per-iteration flux and relative L2 change."""
+        import torch
+
+        if self._plan is None:
+            raise RuntimeError("plan destroyed")
+        if scratch is None:
+            scratch = torch.empty(self.scratch_bytes, dtype=torch.uint8, device=observed.device)
+        o, e = _device_view(observed), _device_view(estimate)
+        stats_ptr = None
+        if stats is not None:
+            if stats.dtype != torch.float64 or not stats.is_cuda or stats.numel() < 2 * iterations:
+                raise ValueError("stats must be a CUDA float64 tensor with 2*iterations entries")
+            stats_ptr = stats.data_ptr()
+        check(lib().iane_gb_rl_run(self._plan, ctypes.byref(o), ctypes.byref(e), int(iterations),
+                                   ctypes.c_float(epsilon), int(init), scratch.data_ptr(), scratch.numel(),
+                                   stats_ptr, _stream_handle(stream)))
+        return estimate
+
+    def run_host(self, observed_host, estimate_host, iterations: int, epsilon: float = 1e-6,
+                 init: int = abi.RL_INIT_OBSERVED, scratch=None, stream=None):
+        """End-to-end run from host (ideally pinned) CPU tensors; blocks until done."""
+        import torch
+
+        u8 = observed_host.dtype == torch.uint8
+        if scratch is None:
+            scratch = torch.empty(self.host_scratch_bytes(u8), dtype=torch.uint8, device="cuda")
+        assert estimate_host.dtype == torch.float32 and estimate_host.is_contiguous()
+        assert observed_host.is_contiguous() and not observed_host.is_cuda
+        check(lib().iane_gb_rl_run_host(self._plan, observed_host.data_ptr(), abi.U8 if u8 else abi.F32,
+                                        estimate_host.data_ptr(), int(iterations), ctypes.c_float(epsilon),
+                                        int(init), scratch.data_ptr(), scratch.numel(), _stream_handle(stream)))
+        return estimate_host
+
+    def close(self) -> None:
+        if self._plan is not None:
+            lib().iane_gb_rl_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,96 @@
+"""Loader for ``libiane_gb300.so`` (the C ABI in ``include/iane_gb/capi.h``).
+
+There is no fallback: if the library is missing or fails to load, every entry point
+raises. Build it with ``python -m iane_gb300.build``.
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+from . import abi
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libiane_gb300.so"
+HEADER = HERE.parent / "include" / "iane_gb" / "capi.h"
+
+_VIEW_P = ctypes.POINTER(abi.View)
+_lib = None
+
+
+class IaneError(RuntimeError):
+    """A negative status from the C ABI; ``status`` holds the code."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status}: {abi.STATUS_NAMES.get(status, 'unknown')})")
+        self.status = status
+
+
+class IaneInvalidArgument(IaneError, ValueError):
+    """The reference throws std::invalid_argument for these."""
+
+
+class IaneLengthError(IaneError, ValueError):
+    """The reference throws std::length_error for an undersized scratch reservation."""
+
+
+def header_functions() -> list[str]:
+    """Names of the functions ``capi.h`` declares."""
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t)\s+(iane_gb_\w+)\s*\(", text, flags=re.M)))
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m iane_gb300.build`")
+    l = ctypes.CDLL(str(LIB_PATH))
+    vp, cvp, i32p = ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)
+    l.iane_gb_abi_version.argtypes = []
+    l.iane_gb_abi_version.restype = ctypes.c_int
+    l.iane_gb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    l.iane_gb_last_error.restype = ctypes.c_size_t
+    l.iane_gb_device_status.argtypes = [vp]
+    l.iane_gb_device_status.restype = ctypes.c_int
+    l.iane_gb_convolve.argtypes = [_VIEW_P, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_uint, vp]
+    l.iane_gb_convolve.restype = ctypes.c_int
+    l.iane_gb_convolve_separable.argtypes = [_VIEW_P, ctypes.POINTER(_VIEW_P), _VIEW_P, ctypes.c_int, vp]
+    l.iane_gb_convolve_separable.restype = ctypes.c_int
+    l.iane_gb_rl_prepare.argtypes = [_VIEW_P, ctypes.c_int, i32p, vp, ctypes.POINTER(vp)]
+    l.iane_gb_rl_prepare.restype = ctypes.c_int
+    l.iane_gb_rl_scratch_bytes.argtypes = [cvp]
+    l.iane_gb_rl_scratch_bytes.restype = ctypes.c_size_t
+    l.iane_gb_rl_run.argtypes = [vp, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp,
+                                 ctypes.c_size_t, vp, vp]
+    l.iane_gb_rl_run.restype = ctypes.c_int
+    l.iane_gb_rl_host_scratch_bytes.argtypes = [cvp, ctypes.c_int]
+    l.iane_gb_rl_host_scratch_bytes.restype = ctypes.c_size_t
+    l.iane_gb_rl_run_host.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp,
+                                      ctypes.c_size_t, vp]
+    l.iane_gb_rl_run_host.restype = ctypes.c_int
+    l.iane_gb_rl_destroy.argtypes = [vp]
+    l.iane_gb_rl_destroy.restype = ctypes.c_int
+    if l.iane_gb_abi_version() != abi.ABI_VERSION:
+        raise RuntimeError("libiane_gb300.so ABI version mismatch; rebuild it")
+    _lib = l
+    return l
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    lib().iane_gb_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int) -> None:
+    if status == abi.OK:
+        return
+    message = last_error()
+    if status == abi.INVALID_ARGUMENT:
+        raise IaneInvalidArgument(status, message)
+    if status == abi.LENGTH_ERROR:
+        raise IaneLengthError(status, message)
+    raise IaneError(status, message)

@@ -1,0 +1,234 @@
+// Shared host/device helpers for the iane_gb kernels (sm_103a only).
+#pragma once
+
+#include "../../include/iane_gb/capi.h"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ != 1030)
+#error "iane_gb kernels are written for sm_103a only"
+#endif
+
+namespace iane_gb {
+
+// ------------------------------------------------------------------------------------
+// host-side error state (one message per host thread, read by iane_gb_last_error)
+
+void set_error(const std::string& message);
+int fail(int status, const std::string& message);
+int cuda_fail(cudaError_t error, const char* what);
+
+#define IANE_GB_CUDA(call, what)                          \
+	do {                                                  \
+		const cudaError_t iane_gb_err_ = (call);          \
+		if (iane_gb_err_ != cudaSuccess) {                \
+			return ::iane_gb::cuda_fail(iane_gb_err_, what); \
+		}                                                 \
+	} while (0)
+
+int dtype_size(int dtype);
+const char* dtype_name(int dtype);
+
+// ------------------------------------------------------------------------------------
+// views
+
+// A rank-3 normalised view: unused axes have extent 1 and stride 0.
+struct DevView {
+	char* ptr;
+	int dtype;
+	int rank;
+	int ext[3];
+	long long stride[3];
+};
+
+// Validate a C-ABI view and normalise it to rank 3. Returns 0 or a negative status.
+int normalise_view(const iane_gb_view* view, const char* name, DevView* out);
+
+__host__ __device__ inline long long element_count(const DevView& v)
+{
+	return static_cast<long long>(v.ext[0]) * v.ext[1] * v.ext[2];
+}
+
+// True when axis 0 is contiguous and rows/planes are packed with a pitch that is a
+// multiple of 16 bytes and the base pointer is 16-byte aligned.
+bool rows_aligned16(const DevView& v);
+
+// ------------------------------------------------------------------------------------
+// device-side element access
+
+template<class T> struct dtype_of;
+template<> struct dtype_of<uint8_t> { static constexpr int value = IANE_GB_U8; };
+template<> struct dtype_of<uint16_t> { static constexpr int value = IANE_GB_U16; };
+template<> struct dtype_of<int16_t> { static constexpr int value = IANE_GB_I16; };
+template<> struct dtype_of<int32_t> { static constexpr int value = IANE_GB_I32; };
+template<> struct dtype_of<float> { static constexpr int value = IANE_GB_F32; };
+template<> struct dtype_of<double> { static constexpr int value = IANE_GB_F64; };
+template<> struct dtype_of<__nv_bfloat16> { static constexpr int value = IANE_GB_BF16; };
+
+template<class T> __device__ __forceinline__ float to_float(T v) { return static_cast<float>(v); }
+template<> __device__ __forceinline__ float to_float<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template<class T> __device__ __forceinline__ double to_double(T v) { return static_cast<double>(v); }
+template<> __device__ __forceinline__ double to_double<__nv_bfloat16>(__nv_bfloat16 v)
+{
+	return static_cast<double>(__bfloat162float(v));
+}
+
+// The reference's conversion of an accumulated sum to the destination element
+// (include/iane/algorithms/convolution.hpp:51-75): bytes round half up and saturate,
+// other integers saturate with NaN -> 0, floating point is a plain cast.
+template<class TD> __device__ __forceinline__ TD convert_sum(double sum);
+template<> __device__ __forceinline__ uint8_t convert_sum<uint8_t>(double sum)
+{
+	if (!(sum > 0.0)) return 0;
+	if (sum >= 255.0) return 255;
+	const unsigned int integer = static_cast<unsigned int>(sum);
+	return static_cast<uint8_t>(integer + (sum - integer >= 0.5));
+}
+template<class TI> __device__ __forceinline__ TI saturate_integral(double sum, double lo, double hi, TI lov, TI hiv)
+{
+	if (sum != sum) return TI(0);
+	if (sum <= lo) return lov;
+	if (sum >= hi) return hiv;
+	return static_cast<TI>(sum);
+}
+template<> __device__ __forceinline__ uint16_t convert_sum<uint16_t>(double sum)
+{
+	return saturate_integral<uint16_t>(sum, 0.0, 65535.0, 0, 65535);
+}
+template<> __device__ __forceinline__ int16_t convert_sum<int16_t>(double sum)
+{
+	return saturate_integral<int16_t>(sum, -32768.0, 32767.0, -32768, 32767);
+}
+template<> __device__ __forceinline__ int32_t convert_sum<int32_t>(double sum)
+{
+	return saturate_integral<int32_t>(sum, -2147483648.0, 2147483647.0, INT32_MIN, INT32_MAX);
+}
+template<> __device__ __forceinline__ float convert_sum<float>(double sum) { return static_cast<float>(sum); }
+template<> __device__ __forceinline__ double convert_sum<double>(double sum) { return sum; }
+
+// Border rule for one coordinate: returns false if the sample is the zero value.
+// clamp/zero follow include/iane/locator/image_locator.hpp:44-52; mirror is half-sample
+// symmetric with period 2n.
+__device__ __forceinline__ bool map_coord(int c, int n, int border, int& out)
+{
+	if (c >= 0 && c < n) {
+		out = c;
+		return true;
+	}
+	if (border == IANE_GB_BORDER_ZERO) {
+		return false;
+	}
+	if (border == IANE_GB_BORDER_CLAMP) {
+		out = c < 0 ? 0 : n - 1;
+		return true;
+	}
+	const int period = 2 * n;
+	int m = c % period;
+	if (m < 0) m += period;
+	out = m < n ? m : period - 1 - m;
+	return true;
+}
+
+template<class T>
+__device__ __forceinline__ const T* element_ptr(const DevView& v, int x, int y, int z)
+{
+	return reinterpret_cast<const T*>(v.ptr + x * v.stride[0] + y * v.stride[1] + z * v.stride[2]);
+}
+
+// ------------------------------------------------------------------------------------
+// device status word: bounded waits that give up record a code here instead of trapping
+
+// `status` points at a library-owned device word (see device_status_ptr()).
+__device__ __forceinline__ void report_device_status(int* status, int code)
+{
+	atomicCAS(status, 0, code);
+}
+
+// ------------------------------------------------------------------------------------
+// TMA / mbarrier helpers (inline PTX, sm_90+ forms that sm_103a supports)
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+	return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init()
+{
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+		: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+	uint32_t done;
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		"selp.u32 %0, 1, 0, p;\n\t}"
+		: "=r"(done)
+		: "r"(smem_addr(bar)), "r"(parity)
+		: "memory");
+	return done != 0;
+}
+
+// Bounded wait on an mbarrier phase. try_wait suspends for a hardware-chosen interval per
+// call, so the limit corresponds to well over a second. Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+	for (uint32_t i = 0; i < (1u << 24); ++i) {
+		if (mbar_try_wait(bar, parity)) {
+			return true;
+		}
+	}
+	return false;
+}
+
+// 3-D tiled TMA load into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+	asm volatile(
+		"cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+		::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+		: "memory");
+}
+
+// 4-byte asynchronous global->shared copy; src_bytes = 0 writes zero.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, int src_bytes)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes)
+		: "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template<int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// ------------------------------------------------------------------------------------
+// host: tensor maps
+
+// Encode a 3-D f32 tensor map over a packed-pitch buffer: dims (nx, ny, nz), byte pitches
+// row_pitch (dim 1) and plane_pitch (dim 2), box (bx, by, 1), zero fill out of bounds.
+int encode_tensor_map_f32(CUtensorMap* map, const void* base, int nx, int ny, int nz,
+	long long row_pitch, long long plane_pitch, int bx, int by);
+
+int device_sm_count();
+
+// Device address of the status word of the current device (one int per device, zero while
+// no bounded wait has given up). Null on failure, with the error recorded.
+int* device_status_ptr();
+
+}  // namespace iane_gb

@@ -1,0 +1,279 @@
+// Register-tiled FP32 direct convolution core, shared by iane_gb_convolve's fast path and
+// the two fused Richardson-Lucy passes.
+//
+// Geometry (one output plane z per block, kernel planes streamed through shared memory):
+//   * a warp is 4 (x) x 8 (y) lanes; each lane owns kRX=8 consecutive x by kRY=4
+//     consecutive y outputs, so a warp covers 32x32 and a block of WX x WY warps covers
+//     (32 WX) x (32 WY) outputs;
+//   * for each kernel plane qz the input halo tile of that plane, (TX + 2 rx) x (TY + 2 ry)
+//     floats, is staged in shared memory -- by one TMA (cp.async.bulk.tensor, zero fill
+//     outside the image) when the border is zero and the buffer is TMA-addressable, else by
+//     4-byte cp.async with the border rule applied per element -- double buffered, so the
+//     next plane lands while this one is consumed;
+//   * a lane walks the RY + 2 ry input rows it needs; each row segment (8 + 2 rx floats) is
+//     read once with 128-bit shared loads into registers and feeds every (output row j,
+//     kernel row b) pair that uses it: 8 x KX FMAs per (j, b) against a kernel row that is
+//     read as a warp-uniform broadcast.
+// Per kernel plane each output accumulates its ky*kx taps into a plane partial that is
+// added to the total afterwards (two-level FP32 summation), which keeps the rounding error
+// of a 1575-tap sum near 1e-6 relative.
+//
+// Coordinates follow the reference's convolution_filter (include/iane/algorithms/
+// convolution.hpp:37-45): out[p] = sum_q K[q] * in[p + size/2 - q].
+#pragma once
+
+#include "common.cuh"
+
+namespace iane_gb {
+
+constexpr int kRX = 8;
+constexpr int kRY = 4;
+
+template<int KX>
+struct TileGeom {
+	static constexpr int rx = KX / 2;
+	static constexpr int RXA = (rx + 3) & ~3;              // x halo rounded to a 16-byte boundary
+	static constexpr int D = RXA - rx;                      // segment lead-in
+	static constexpr int SEGN = (D + kRX + KX - 1 + 3) & ~3; // floats per row segment (multiple of 4)
+	static constexpr int KXP = (KX + 3) & ~3;               // padded kernel row in shared memory
+};
+
+template<int KX, int WX>
+struct TileWidth {
+	static constexpr int TX = 32 * WX;
+	static constexpr int W = TX - kRX + TileGeom<KX>::SEGN;  // columns read
+	static constexpr int P = (W % 8 == 0) ? W + 4 : W;        // pitch, = 4 mod 8 floats
+};
+
+struct TileArgs {
+	// source of the halo tiles (f32), used by the cp.async path
+	const char* src;
+	long long s_stride[3];
+	int nx, ny, nz;
+	// kernel: kx is the template KX; f32 device view
+	int ky, kz;
+	const char* kernel;
+	long long k_stride[3];
+	int border;
+	int* status; // device status word for bounded waits
+};
+
+// Shared memory bytes of one launch.
+template<int KX, int WX, int WY>
+inline size_t tile_smem_bytes(int ky, int kz)
+{
+	const int H = 32 * WY + 2 * (ky / 2);
+	const size_t plane = (static_cast<size_t>(TileWidth<KX, WX>::P) * H * 4 + 127) & ~size_t(127);
+	const size_t psf = (static_cast<size_t>(kz) * ky * TileGeom<KX>::KXP * 4 + 127) & ~size_t(127);
+	return 2 * plane + psf + 16;
+}
+
+template<int KX, int WX, int WY, bool TMA, class Epi>
+__global__ void __launch_bounds__(32 * WX * WY)
+	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const Epi epi_in)
+{
+	using G = TileGeom<KX>;
+	constexpr int TX = 32 * WX;
+	constexpr int TY = 32 * WY;
+	constexpr int P = TileWidth<KX, WX>::P;
+	constexpr int W = TileWidth<KX, WX>::W;
+	constexpr int NT = 32 * WX * WY;
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+
+	const int ky = a.ky, kz = a.kz;
+	const int ry = ky / 2, rz = kz / 2;
+	const int H = TY + 2 * ry;
+	const int plane_floats = ((P * H + 31) & ~31);
+	float* tiles = reinterpret_cast<float*>(smem_raw);
+	float* psf_s = tiles + 2 * plane_floats;
+	const int psf_floats = ((kz * ky * G::KXP + 31) & ~31);
+	uint64_t* bars = reinterpret_cast<uint64_t*>(psf_s + psf_floats);
+
+	const int tid = threadIdx.x;
+	const int lane = tid & 31, warp = tid >> 5;
+	const int tx_b = (warp % WX) * 4 + (lane & 3);
+	const int ty_b = (warp / WX) * 8 + (lane >> 2);
+	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
+
+	// Kernel planes that touch the image: all of them except, for a zero border, planes
+	// whose input plane lies outside (those contribute only zero samples).
+	int qz_lo = 0, qz_hi = kz - 1;
+	if (a.border == IANE_GB_BORDER_ZERO) {
+		qz_lo = max(0, z + rz - (a.nz - 1));
+		qz_hi = min(kz - 1, z + rz);
+	}
+	const int nplanes = qz_hi - qz_lo + 1;
+
+	for (int i = tid; i < kz * ky * G::KXP; i += NT) {
+		const int qx = i % G::KXP, row = i / G::KXP;
+		const int qy = row % ky, qz = row / ky;
+		float v = 0.0f;
+		if (qx < KX) {
+			v = *reinterpret_cast<const float*>(a.kernel + qx * a.k_stride[0] + qy * a.k_stride[1] + qz * a.k_stride[2]);
+		}
+		psf_s[i] = v;
+	}
+	if constexpr (TMA) {
+		if (tid == 0) {
+			mbar_init(&bars[0], 1);
+			mbar_init(&bars[1], 1);
+			fence_barrier_init();
+		}
+	}
+	__syncthreads();
+
+	auto issue = [&](int p) {
+		float* dst = tiles + (p & 1) * plane_floats;
+		const int qz = qz_lo + p;
+		if constexpr (TMA) {
+			if (tid == 0) {
+				mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(P * H * 4));
+				tma_load_3d(dst, &tmap, x0 - G::RXA, y0 - ry, z + rz - qz, &bars[p & 1]);
+			}
+		} else {
+			int zi = 0;
+			const bool zok = map_coord(z + rz - qz, a.nz, a.border, zi);
+			const char* plane = a.src + zi * a.s_stride[2];
+			for (int i = tid; i < W * H; i += NT) {
+				const int col = i % W, row = i / W;
+				int xi = 0, yi = 0;
+				const bool ok = zok && map_coord(x0 - G::RXA + col, a.nx, a.border, xi) &&
+					map_coord(y0 - ry + row, a.ny, a.border, yi);
+				const char* src = ok ? plane + xi * a.s_stride[0] + yi * a.s_stride[1] : a.src;
+				cp_async4(dst + row * P + col, src, ok ? 4 : 0);
+			}
+			cp_async_commit();
+		}
+	};
+
+	float acc[kRY][kRX];
+#pragma unroll
+	for (int j = 0; j < kRY; ++j)
+#pragma unroll
+		for (int i = 0; i < kRX; ++i) acc[j][i] = 0.0f;
+
+	bool ok = true;
+	if (nplanes > 0) issue(0);
+	if (nplanes > 1) issue(1);
+	for (int p = 0; p < nplanes; ++p) {
+		if constexpr (TMA) {
+			if (ok && !mbar_wait_bounded(&bars[p & 1], (p >> 1) & 1)) {
+				ok = false;
+				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
+			}
+		} else {
+			if (p + 1 < nplanes) {
+				cp_async_wait<1>();
+			} else {
+				cp_async_wait<0>();
+			}
+			__syncthreads();
+		}
+		const float* tile = tiles + (p & 1) * plane_floats + (kRY * ty_b) * P + kRX * tx_b;
+		const float* kplane = psf_s + (qz_lo + p) * ky * G::KXP;
+		float part[kRY][kRX];
+#pragma unroll
+		for (int j = 0; j < kRY; ++j)
+#pragma unroll
+			for (int i = 0; i < kRX; ++i) part[j][i] = 0.0f;
+
+		const int rows = kRY + 2 * ry;
+#pragma unroll 1
+		for (int r = 0; r < rows; ++r) {
+			float seg[G::SEGN];
+			const float4* srow = reinterpret_cast<const float4*>(tile + r * P);
+#pragma unroll
+			for (int m = 0; m < G::SEGN / 4; ++m) {
+				const float4 v = srow[m];
+				seg[4 * m + 0] = v.x;
+				seg[4 * m + 1] = v.y;
+				seg[4 * m + 2] = v.z;
+				seg[4 * m + 3] = v.w;
+			}
+#pragma unroll
+			for (int j = 0; j < kRY; ++j) {
+				const int b = j + 2 * ry - r;
+				if (b >= 0 && b < ky) {
+					const float4* krow = reinterpret_cast<const float4*>(kplane + b * G::KXP);
+					float k[G::KXP];
+#pragma unroll
+					for (int m = 0; m < G::KXP / 4; ++m) {
+						const float4 v = krow[m];
+						k[4 * m + 0] = v.x;
+						k[4 * m + 1] = v.y;
+						k[4 * m + 2] = v.z;
+						k[4 * m + 3] = v.w;
+					}
+#pragma unroll
+					for (int q = 0; q < KX; ++q) {
+#pragma unroll
+						for (int i = 0; i < kRX; ++i) {
+							part[j][i] = fmaf(k[q], seg[G::D + i + 2 * G::rx - q], part[j][i]);
+						}
+					}
+				}
+			}
+		}
+#pragma unroll
+		for (int j = 0; j < kRY; ++j)
+#pragma unroll
+			for (int i = 0; i < kRX; ++i) acc[j][i] += part[j][i];
+
+		__syncthreads(); // every lane is done with this buffer
+		if (p + 2 < nplanes) issue(p + 2);
+	}
+
+	Epi epi = epi_in;
+	const int xo = x0 + kRX * tx_b;
+	const int yo = y0 + kRY * ty_b;
+#pragma unroll
+	for (int j = 0; j < kRY; ++j) {
+		epi.row(xo, yo + j, z, acc[j]);
+	}
+	epi.finish();
+}
+
+// Launch helper: grid = tiles over (x, y) and one block per output plane.
+template<int KX, int WX, int WY, bool TMA, class Epi>
+int launch_tile(const CUtensorMap& map, const TileArgs& a, const Epi& epi, cudaStream_t stream)
+{
+	auto kernel = conv_tile_kernel<KX, WX, WY, TMA, Epi>;
+	const size_t smem = tile_smem_bytes<KX, WX, WY>(a.ky, a.kz);
+	IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+		"tiled convolution: set shared memory size");
+	const dim3 grid((a.nx + 32 * WX - 1) / (32 * WX), (a.ny + 32 * WY - 1) / (32 * WY), a.nz);
+	kernel<<<grid, 32 * WX * WY, smem, stream>>>(map, a, epi);
+	IANE_GB_CUDA(cudaGetLastError(), "tiled convolution: launch");
+	return IANE_GB_OK;
+}
+
+// Plain f32 store epilogue for iane_gb_convolve.
+struct EpiStoreF32 {
+	char* dst;
+	long long stride[3];
+	int nx, ny;
+	int vec4; // rows start 16-byte aligned and axis 0 is packed
+
+	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[kRX]) const
+	{
+		if (y >= ny) {
+			return;
+		}
+		char* base = dst + y * stride[1] + z * stride[2];
+		if (vec4 && xo + kRX <= nx) {
+			float4* p = reinterpret_cast<float4*>(base + xo * 4LL);
+			p[0] = make_float4(v[0], v[1], v[2], v[3]);
+			p[1] = make_float4(v[4], v[5], v[6], v[7]);
+			return;
+		}
+#pragma unroll
+		for (int i = 0; i < kRX; ++i) {
+			if (xo + i < nx) {
+				*reinterpret_cast<float*>(base + (xo + i) * stride[0]) = v[i];
+			}
+		}
+	}
+	__device__ __forceinline__ void finish() const {}
+};
+
+}  // namespace iane_gb

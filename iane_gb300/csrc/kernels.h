@@ -1,0 +1,23 @@
+// Host-side launchers shared between the library's translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace iane_gb {
+
+// Generic direct convolution (conv_generic.cu): any supported element types, border and
+// strides; exact = FP64 fma in kernel raster order.
+int launch_conv_generic(const DevView& src, const DevView& kernel, const DevView& dst, int border, bool exact,
+	cudaStream_t stream);
+
+// Register-tiled FP32 convolution (conv_f32.cu). Returns IANE_GB_UNSUPPORTED (without
+// recording an error) when the shapes are outside what the tiled path takes, so that the
+// caller falls back to the generic kernel.
+int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevView& dst, int border,
+	cudaStream_t stream);
+
+// Fused separable FP32 convolution (separable.cu).
+int launch_conv_separable(const DevView& src, const DevView* taps, const DevView& dst, int border,
+	cudaStream_t stream);
+
+}  // namespace iane_gb

@@ -1,0 +1,556 @@
+// Richardson-Lucy as a prepared algorithm: plan (prepare), scratch sizing and run.
+//
+// Reference: examples/rl_deconvolution/main.cu:51-81 (prepare_rl and the iteration),
+// include/iane/execution/prepared.hpp:120-146 (prepare -> scratch_bytes, run with scratch),
+// include/iane/execution/run_on.hpp:86-178 (host staging for the end-to-end entry point).
+//
+// HBM layout of the scratch (each part 256-byte aligned):
+//   ratio  : f32 work image, rows padded to a multiple of 4 floats (TMA-addressable)
+//   est    : f32 work estimate, same layout (unused when the caller's estimate view already
+//            has that layout -- then the passes update it in place)
+//   parts  : 3 doubles per block of pass B (statistics partials)
+//   misc   : block-completion counter and the flat-start value
+#include "kernels.h"
+#include "rl.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+struct iane_gb_rl_plan {
+	int rank;
+	int ext[3];
+	int k[3];
+	int device;
+	float* d_psf;  // packed PSF
+	float* d_adj;  // packed adjoint (every axis reversed)
+	int* d_cls;    // sensitivity class per coordinate: x then y then z
+	float* d_sens; // sensitivity per class triple
+	int ccount[3];
+	int ilo[3], ihi[3];
+	float s_interior;
+	long long pitch;       // floats per work-image row
+	size_t image_bytes;    // one work image, rounded to 256
+	size_t parts_bytes;
+	size_t scratch_bytes;
+	bool small_tiles;
+	long long pass_blocks;
+};
+
+namespace iane_gb {
+
+int launch_rl_pass_a_lo(int, bool, const CUtensorMap&, const TileArgs&, const EpiRatio&, cudaStream_t);
+int launch_rl_pass_a_hi(int, bool, const CUtensorMap&, const TileArgs&, const EpiRatio&, cudaStream_t);
+int launch_rl_pass_b_lo(int, bool, const CUtensorMap&, const TileArgs&, const EpiUpdate&, cudaStream_t);
+int launch_rl_pass_b_hi(int, bool, const CUtensorMap&, const TileArgs&, const EpiUpdate&, cudaStream_t);
+
+int launch_rl_pass_a(int kx, bool small, const CUtensorMap& map, const TileArgs& a, const EpiRatio& e,
+	cudaStream_t stream)
+{
+	return kx <= 15 ? launch_rl_pass_a_lo(kx, small, map, a, e, stream) : launch_rl_pass_a_hi(kx, small, map, a, e, stream);
+}
+
+int launch_rl_pass_b(int kx, bool small, const CUtensorMap& map, const TileArgs& a, const EpiUpdate& e,
+	cudaStream_t stream)
+{
+	return kx <= 15 ? launch_rl_pass_b_lo(kx, small, map, a, e, stream) : launch_rl_pass_b_hi(kx, small, map, a, e, stream);
+}
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+__global__ void gather_f32_kernel(DevView src, float* dst)
+{
+	const long long n = element_count(src);
+	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
+		const int x = static_cast<int>(i % src.ext[0]);
+		const int y = static_cast<int>((i / src.ext[0]) % src.ext[1]);
+		const int z = static_cast<int>(i / (static_cast<long long>(src.ext[0]) * src.ext[1]));
+		dst[i] = *element_ptr<float>(src, x, y, z);
+	}
+}
+
+// Observed-based start (main.cu:12-19) or flat start, into the work estimate.
+__global__ void rl_init_kernel(DevView obs, float* est, long long pitch, long long plane, float eps, int mode,
+	const float* start)
+{
+	const int nx = obs.ext[0], ny = obs.ext[1], nz = obs.ext[2];
+	const long long n = static_cast<long long>(nx) * ny * nz;
+	const float flat = mode == IANE_GB_RL_INIT_MEAN ? *start : 0.0f;
+	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
+		const int x = static_cast<int>(i % nx);
+		const int y = static_cast<int>((i / nx) % ny);
+		const int z = static_cast<int>(i / (static_cast<long long>(nx) * ny));
+		float v = flat;
+		if (mode == IANE_GB_RL_INIT_OBSERVED) {
+			const char* p = obs.ptr + x * obs.stride[0] + y * obs.stride[1] + z * obs.stride[2];
+			const float o = obs.dtype == IANE_GB_U8 ? static_cast<float>(*reinterpret_cast<const uint8_t*>(p))
+				: *reinterpret_cast<const float*>(p);
+			v = o > eps ? o : eps;
+		}
+		est[z * plane + y * pitch + x] = v;
+	}
+}
+
+// Sum of the observed image in FP64; the last block writes max(mean, eps) to *start.
+__global__ void rl_mean_kernel(DevView obs, double* partials, unsigned int* counter, float* start, float eps)
+{
+	const int nx = obs.ext[0], ny = obs.ext[1], nz = obs.ext[2];
+	const long long n = static_cast<long long>(nx) * ny * nz;
+	double s = 0.0;
+	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
+		const int x = static_cast<int>(i % nx);
+		const int y = static_cast<int>((i / nx) % ny);
+		const int z = static_cast<int>(i / (static_cast<long long>(nx) * ny));
+		const char* p = obs.ptr + x * obs.stride[0] + y * obs.stride[1] + z * obs.stride[2];
+		s += obs.dtype == IANE_GB_U8 ? static_cast<double>(*reinterpret_cast<const uint8_t*>(p))
+			: static_cast<double>(*reinterpret_cast<const float*>(p));
+	}
+	__shared__ double red[32];
+	__shared__ int last;
+	for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t = 0.0;
+		for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += red[w];
+		partials[blockIdx.x] = t;
+		__threadfence();
+		last = atomicAdd(counter, 1u) == gridDim.x - 1;
+	}
+	__syncthreads();
+	if (last && threadIdx.x == 0) {
+		__threadfence();
+		double total = 0.0;
+		for (unsigned int b = 0; b < gridDim.x; ++b) total += __ldcg(&partials[b]);
+		const float mean = static_cast<float>(total / static_cast<double>(n));
+		*start = mean > eps ? mean : eps;
+		*counter = 0u;
+	}
+}
+
+// Copy between the work estimate and a caller view (f32 or u8 via to_gray8).
+__global__ void rl_copy_kernel(float* est, long long pitch, long long plane, DevView view, int to_view)
+{
+	const int nx = view.ext[0], ny = view.ext[1], nz = view.ext[2];
+	const long long n = static_cast<long long>(nx) * ny * nz;
+	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
+		const int x = static_cast<int>(i % nx);
+		const int y = static_cast<int>((i / nx) % ny);
+		const int z = static_cast<int>(i / (static_cast<long long>(nx) * ny));
+		char* p = view.ptr + x * view.stride[0] + y * view.stride[1] + z * view.stride[2];
+		float& e = est[z * plane + y * pitch + x];
+		if (to_view) {
+			if (view.dtype == IANE_GB_U8) {
+				*reinterpret_cast<uint8_t*>(p) = to_gray8(e);
+			} else {
+				*reinterpret_cast<float*>(p) = e;
+			}
+		} else {
+			e = *reinterpret_cast<const float*>(p);
+		}
+	}
+}
+
+int grid_for(long long n)
+{
+	const long long blocks = (n + 255) / 256;
+	const long long cap = 8LL * device_sm_count();
+	return static_cast<int>(blocks < 1 ? 1 : (blocks > cap ? cap : blocks));
+}
+
+// Per-axis sensitivity classes: voxel p sees kernel taps [max(0, p+c-n+1), min(k-1, p+c)].
+void axis_classes(int n, int k, std::vector<int>& cls, std::vector<std::pair<int, int>>& ranges, int& lo, int& hi)
+{
+	const int c = k / 2;
+	cls.assign(n, 0);
+	ranges.clear();
+	lo = c;
+	hi = n - 1 - c;
+	for (int p = 0; p < n; ++p) {
+		const int qlo = p + c - n + 1 > 0 ? p + c - n + 1 : 0;
+		const int qhi = p + c < k - 1 ? p + c : k - 1;
+		int id = -1;
+		for (size_t i = 0; i < ranges.size(); ++i) {
+			if (ranges[i].first == qlo && ranges[i].second == qhi) {
+				id = static_cast<int>(i);
+				break;
+			}
+		}
+		if (id < 0) {
+			id = static_cast<int>(ranges.size());
+			ranges.emplace_back(qlo, qhi);
+		}
+		cls[p] = id;
+	}
+}
+
+bool is_work_layout(const DevView& v, long long pitch)
+{
+	// The caller's estimate can be updated in place when it is f32, packed with our row
+	// pitch and 16-byte aligned.
+	if (v.dtype != IANE_GB_F32 || v.stride[0] != 4 || reinterpret_cast<uintptr_t>(v.ptr) % 16 != 0) return false;
+	if (v.ext[1] > 1 && v.stride[1] != pitch * 4) return false;
+	if (v.ext[2] > 1 && v.stride[2] != pitch * 4 * v.ext[1]) return false;
+	return true;
+}
+
+}  // namespace
+}  // namespace iane_gb
+
+using namespace iane_gb;
+
+extern "C" {
+
+int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent, void* stream, iane_gb_rl_plan** out)
+{
+	if (!out || !extent) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: null argument");
+	}
+	*out = nullptr;
+	DevView k{};
+	int status = normalise_view(psf, "rl_prepare psf", &k);
+	if (status) return status;
+	if (rank < 1 || rank > 3 || k.rank != rank) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: PSF rank must equal the image rank (1..3)");
+	}
+	if (k.dtype != IANE_GB_F32) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: the PSF must be f32");
+	}
+	int ext[3] = {1, 1, 1};
+	for (int i = 0; i < rank; ++i) {
+		if (k.ext[i] <= 0 || k.ext[i] % 2 == 0) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "Convolution requires positive odd kernel dimensions");
+		}
+		if (extent[i] < 0) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: negative image extent");
+		}
+		ext[i] = extent[i];
+	}
+	if (k.ext[0] > 31 || k.ext[1] > 63) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: PSF wider than 31 along axis 0 or 63 along axis 1");
+	}
+	const long long taps = static_cast<long long>(k.ext[0]) * k.ext[1] * k.ext[2];
+	if (taps * ((k.ext[0] + 3) & ~3) / k.ext[0] * 4 > 96 * 1024) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: PSF too large for shared memory");
+	}
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	auto* plan = new iane_gb_rl_plan{};
+	plan->rank = rank;
+	for (int i = 0; i < 3; ++i) {
+		plan->ext[i] = ext[i];
+		plan->k[i] = k.ext[i];
+	}
+	cudaGetDevice(&plan->device);
+	auto cleanup = [&](int code) {
+		iane_gb_rl_destroy(plan);
+		return code;
+	};
+	if (cudaMalloc(&plan->d_psf, taps * sizeof(float)) != cudaSuccess ||
+	    cudaMalloc(&plan->d_adj, taps * sizeof(float)) != cudaSuccess) {
+		return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: allocate PSF copies"));
+	}
+	gather_f32_kernel<<<grid_for(taps), 256, 0, st>>>(k, plan->d_psf);
+	std::vector<float> h_psf(taps), h_adj(taps);
+	if (cudaMemcpyAsync(h_psf.data(), plan->d_psf, taps * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+	    cudaStreamSynchronize(st) != cudaSuccess) {
+		return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: read PSF"));
+	}
+	for (long long i = 0; i < taps; ++i) {
+		if (!std::isfinite(h_psf[i])) {
+			return cleanup(fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: PSF coefficients must be finite"));
+		}
+		h_adj[i] = h_psf[taps - 1 - i]; // reverse_copy of the packed PSF (main.cu:106-107)
+	}
+	// Sensitivity = zero-border convolution of an all-ones image with the adjoint
+	// (main.cu:62-64): for finite taps the out-of-range terms fma(0, k, s) leave s unchanged,
+	// so each class sums its in-range taps in raster order with FP64 fma exactly as the
+	// reference's convolution_filter does, then rounds to float.
+	std::vector<int> cls[3];
+	std::vector<std::pair<int, int>> ranges[3];
+	for (int a = 0; a < 3; ++a) {
+		axis_classes(ext[a], k.ext[a], cls[a], ranges[a], plan->ilo[a], plan->ihi[a]);
+		plan->ccount[a] = static_cast<int>(ranges[a].size());
+	}
+	const long long ncls = static_cast<long long>(plan->ccount[0]) * plan->ccount[1] * plan->ccount[2];
+	std::vector<float> table(ncls > 0 ? ncls : 1, 0.0f);
+	plan->s_interior = 0.0f;
+	for (int cz = 0; cz < plan->ccount[2]; ++cz) {
+		for (int cy = 0; cy < plan->ccount[1]; ++cy) {
+			for (int cx = 0; cx < plan->ccount[0]; ++cx) {
+				double sum = 0.0;
+				for (int qz = ranges[2][cz].first; qz <= ranges[2][cz].second; ++qz)
+					for (int qy = ranges[1][cy].first; qy <= ranges[1][cy].second; ++qy)
+						for (int qx = ranges[0][cx].first; qx <= ranges[0][cx].second; ++qx)
+							sum = std::fma(1.0, static_cast<double>(
+								h_adj[(static_cast<long long>(qz) * k.ext[1] + qy) * k.ext[0] + qx]), sum);
+				const float v = static_cast<float>(sum);
+				table[(static_cast<long long>(cz) * plan->ccount[1] + cy) * plan->ccount[0] + cx] = v;
+				bool interior = true;
+				for (int a = 0; a < 3; ++a) {
+					const auto& r = ranges[a][a == 0 ? cx : (a == 1 ? cy : cz)];
+					interior = interior && r.first == 0 && r.second == k.ext[a] - 1;
+				}
+				if (interior) plan->s_interior = v;
+			}
+		}
+	}
+	std::vector<int> all_cls;
+	for (int a = 0; a < 3; ++a) all_cls.insert(all_cls.end(), cls[a].begin(), cls[a].end());
+	if (cudaMalloc(&plan->d_cls, (all_cls.size() + 1) * sizeof(int)) != cudaSuccess ||
+	    cudaMalloc(&plan->d_sens, table.size() * sizeof(float)) != cudaSuccess) {
+		return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: allocate sensitivity tables"));
+	}
+	if (cudaMemcpyAsync(plan->d_adj, h_adj.data(), taps * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	    (!all_cls.empty() && cudaMemcpyAsync(plan->d_cls, all_cls.data(), all_cls.size() * sizeof(int),
+	                         cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+	    cudaMemcpyAsync(plan->d_sens, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice, st) !=
+	        cudaSuccess ||
+	    cudaStreamSynchronize(st) != cudaSuccess) {
+		return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: upload tables"));
+	}
+	// Work-image layout and scratch size.
+	plan->pitch = (static_cast<long long>(ext[0]) + 3) & ~3LL;
+	plan->image_bytes = round_up(static_cast<size_t>(plan->pitch) * ext[1] * ext[2] * sizeof(float), kAlign);
+	const long long big_tiles = static_cast<long long>((ext[0] + 63) / 64) * ((ext[1] + 63) / 64) * ext[2];
+	plan->small_tiles = big_tiles < 2LL * device_sm_count();
+	const int t = plan->small_tiles ? 32 : 64;
+	plan->pass_blocks = static_cast<long long>((ext[0] + t - 1) / t) * ((ext[1] + t - 1) / t) * ext[2];
+	const long long mean_blocks = 8LL * device_sm_count();
+	plan->parts_bytes = round_up(static_cast<size_t>(
+		(plan->pass_blocks * 3 > mean_blocks ? plan->pass_blocks * 3 : mean_blocks) * sizeof(double)), kAlign);
+	plan->scratch_bytes = 2 * plan->image_bytes + plan->parts_bytes + 2 * kAlign;
+	*out = plan;
+	return IANE_GB_OK;
+}
+
+size_t iane_gb_rl_scratch_bytes(const iane_gb_rl_plan* plan)
+{
+	return plan ? plan->scratch_bytes : 0;
+}
+
+int iane_gb_rl_destroy(iane_gb_rl_plan* plan)
+{
+	if (!plan) {
+		return IANE_GB_OK;
+	}
+	cudaFree(plan->d_psf);
+	cudaFree(plan->d_adj);
+	cudaFree(plan->d_cls);
+	cudaFree(plan->d_sens);
+	delete plan;
+	return IANE_GB_OK;
+}
+
+int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const iane_gb_view* estimate,
+	int iterations, float epsilon, int init, void* scratch, size_t scratch_bytes, double* stats, void* stream)
+{
+	if (!plan) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run: null plan");
+	}
+	DevView obs{}, est{};
+	int status = normalise_view(observed, "rl_run observed", &obs);
+	if (status) return status;
+	status = normalise_view(estimate, "rl_run estimate", &est);
+	if (status) return status;
+	if (obs.rank != plan->rank || est.rank != plan->rank) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run: views must have the prepared rank");
+	}
+	for (int i = 0; i < 3; ++i) {
+		if (obs.ext[i] != plan->ext[i] || est.ext[i] != plan->ext[i]) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "rl_run: views must have the prepared extents");
+		}
+	}
+	if (obs.dtype != IANE_GB_F32 && obs.dtype != IANE_GB_U8) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_run: observed image must be f32 or u8");
+	}
+	if (est.dtype != IANE_GB_F32 && est.dtype != IANE_GB_U8) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_run: estimate must be f32 or u8");
+	}
+	if (iterations < 0 || !(epsilon > 0.0f) || !std::isfinite(epsilon)) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "Iterations and finite epsilon must be positive");
+	}
+	if (init < IANE_GB_RL_INIT_OBSERVED || init > IANE_GB_RL_INIT_GIVEN) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run: unknown init mode");
+	}
+	if (init == IANE_GB_RL_INIT_GIVEN && est.dtype != IANE_GB_F32) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run: a given start needs an f32 estimate");
+	}
+	if (!scratch || scratch_bytes < plan->scratch_bytes) {
+		return fail(IANE_GB_LENGTH_ERROR, "Prepared operation exceeded its scratch reservation");
+	}
+	if (element_count(obs) == 0) {
+		return IANE_GB_OK;
+	}
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	char* base = reinterpret_cast<char*>(round_up(reinterpret_cast<uintptr_t>(scratch), kAlign));
+	if (base + 2 * plan->image_bytes + plan->parts_bytes + 8 > static_cast<char*>(scratch) + scratch_bytes) {
+		return fail(IANE_GB_LENGTH_ERROR, "Prepared operation exceeded its scratch reservation");
+	}
+	float* ratio = reinterpret_cast<float*>(base);
+	float* work = reinterpret_cast<float*>(base + plan->image_bytes);
+	double* parts = reinterpret_cast<double*>(base + 2 * plan->image_bytes);
+	unsigned int* counter = reinterpret_cast<unsigned int*>(base + 2 * plan->image_bytes + plan->parts_bytes);
+	float* start = reinterpret_cast<float*>(counter + 1);
+	const int nx = plan->ext[0], ny = plan->ext[1], nz = plan->ext[2];
+	const long long pitch = plan->pitch, plane = pitch * ny;
+	const bool in_place = is_work_layout(est, pitch);
+	float* e_work = in_place ? reinterpret_cast<float*>(est.ptr) : work;
+	const long long n = static_cast<long long>(nx) * ny * nz;
+
+	IANE_GB_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned int), st), "rl_run: clear counter");
+	if (init == IANE_GB_RL_INIT_GIVEN) {
+		if (!in_place) {
+			rl_copy_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est, 0);
+		}
+	} else {
+		if (init == IANE_GB_RL_INIT_MEAN) {
+			rl_mean_kernel<<<grid_for(n), 256, 0, st>>>(obs, parts, counter, start, epsilon);
+		}
+		rl_init_kernel<<<grid_for(n), 256, 0, st>>>(obs, e_work, pitch, plane, epsilon, init, start);
+	}
+	IANE_GB_CUDA(cudaGetLastError(), "rl_run: launch init");
+
+	int* dstatus = device_status_ptr();
+	if (!dstatus) return IANE_GB_CUDA_ERROR;
+	const int kx = plan->k[0];
+	const int wx = plan->small_tiles ? 1 : 2;
+	const int box_w = tile_pitch(kx, wx);
+	const int box_h = 32 * wx + 2 * (plan->k[1] / 2);
+	CUtensorMap map_est{}, map_ratio{};
+	status = encode_tensor_map_f32(&map_est, e_work, nx, ny, nz, pitch * 4, plane * 4, box_w, box_h);
+	if (status) return status;
+	status = encode_tensor_map_f32(&map_ratio, ratio, nx, ny, nz, pitch * 4, plane * 4, box_w, box_h);
+	if (status) return status;
+
+	TileArgs ta{};
+	ta.nx = nx;
+	ta.ny = ny;
+	ta.nz = nz;
+	ta.ky = plan->k[1];
+	ta.kz = plan->k[2];
+	ta.k_stride[0] = 4;
+	ta.k_stride[1] = 4LL * plan->k[0];
+	ta.k_stride[2] = 4LL * plan->k[0] * plan->k[1];
+	ta.border = IANE_GB_BORDER_ZERO;
+	ta.status = dstatus;
+	TileArgs tb = ta;
+	ta.kernel = reinterpret_cast<const char*>(plan->d_psf);
+	tb.kernel = reinterpret_cast<const char*>(plan->d_adj);
+
+	EpiRatio ea{};
+	ea.ratio = ratio;
+	ea.pitch = pitch;
+	ea.plane = plane;
+	ea.obs = obs.ptr;
+	for (int i = 0; i < 3; ++i) ea.os[i] = obs.stride[i];
+	ea.obs_u8 = obs.dtype == IANE_GB_U8;
+	ea.eps = epsilon;
+	ea.nx = nx;
+	ea.ny = ny;
+
+	EpiUpdate eb{};
+	eb.est = e_work;
+	eb.pitch = pitch;
+	eb.plane = plane;
+	eb.eps = epsilon;
+	eb.nx = nx;
+	eb.ny = ny;
+	eb.nz = nz;
+	eb.cls = plan->d_cls;
+	eb.sens = plan->d_sens;
+	eb.cx_count = plan->ccount[0];
+	eb.cy_count = plan->ccount[1];
+	for (int i = 0; i < 3; ++i) {
+		eb.ilo[i] = plan->ilo[i];
+		eb.ihi[i] = plan->ihi[i];
+		eb.outs[i] = est.stride[i];
+	}
+	eb.s_interior = plan->s_interior;
+	eb.partials = parts;
+	eb.counter = counter;
+	eb.out = est.ptr;
+	eb.out_u8 = est.dtype == IANE_GB_U8;
+
+	for (int it = 0; it < iterations; ++it) {
+		status = launch_rl_pass_a(kx, plan->small_tiles, map_est, ta, ea, st);
+		if (status) return status;
+		eb.want_stats = stats != nullptr;
+		eb.stats = stats ? stats + 2 * it : nullptr;
+		eb.write_out = (!in_place && it == iterations - 1) ? 1 : 0;
+		status = launch_rl_pass_b(kx, plan->small_tiles, map_ratio, tb, eb, st);
+		if (status) return status;
+	}
+	if (iterations == 0 && !in_place) {
+		rl_copy_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est, 1);
+		IANE_GB_CUDA(cudaGetLastError(), "rl_run: launch copy-out");
+	}
+	return IANE_GB_OK;
+}
+
+size_t iane_gb_rl_host_scratch_bytes(const iane_gb_rl_plan* plan, int observed_dtype)
+{
+	if (!plan) return 0;
+	const size_t n = static_cast<size_t>(plan->ext[0]) * plan->ext[1] * plan->ext[2];
+	const size_t obs = round_up(n * (observed_dtype == IANE_GB_U8 ? 1 : 4), kAlign);
+	const size_t est = round_up(static_cast<size_t>(plan->pitch) * plan->ext[1] * plan->ext[2] * 4, kAlign);
+	return plan->scratch_bytes + obs + est + kAlign;
+}
+
+int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int observed_dtype, float* host_estimate,
+	int iterations, float epsilon, int init, void* scratch, size_t scratch_bytes, void* stream)
+{
+	if (!plan || !host_observed || !host_estimate) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run_host: null argument");
+	}
+	if (observed_dtype != IANE_GB_U8 && observed_dtype != IANE_GB_F32) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_run_host: observed image must be f32 or u8");
+	}
+	if (!scratch || scratch_bytes < iane_gb_rl_host_scratch_bytes(plan, observed_dtype)) {
+		return fail(IANE_GB_LENGTH_ERROR, "Prepared operation exceeded its scratch reservation");
+	}
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	const int nx = plan->ext[0], ny = plan->ext[1], nz = plan->ext[2];
+	const size_t n = static_cast<size_t>(nx) * ny * nz;
+	const int esize = observed_dtype == IANE_GB_U8 ? 1 : 4;
+	char* base = reinterpret_cast<char*>(round_up(reinterpret_cast<uintptr_t>(scratch), kAlign));
+	char* d_obs = base + plan->scratch_bytes;
+	float* d_est = reinterpret_cast<float*>(d_obs + round_up(n * esize, kAlign));
+	const long long pitch = plan->pitch;
+	iane_gb_view ov{}, ev{};
+	ov.ptr = d_obs;
+	ov.dtype = observed_dtype;
+	ov.rank = plan->rank;
+	ev.ptr = d_est;
+	ev.dtype = IANE_GB_F32;
+	ev.rank = plan->rank;
+	long long s = esize;
+	for (int i = 0; i < plan->rank; ++i) {
+		ov.extent[i] = ev.extent[i] = plan->ext[i];
+		ov.stride[i] = s;
+		s *= plan->ext[i];
+	}
+	ev.stride[0] = 4;
+	ev.stride[1] = pitch * 4;
+	ev.stride[2] = pitch * 4 * ny;
+	IANE_GB_CUDA(cudaMemcpyAsync(d_obs, host_observed, n * esize, cudaMemcpyHostToDevice, st), "rl_run_host: upload");
+	if (init == IANE_GB_RL_INIT_GIVEN) {
+		IANE_GB_CUDA(cudaMemcpy2DAsync(d_est, pitch * 4, host_estimate, nx * 4, nx * 4, static_cast<size_t>(ny) * nz,
+			cudaMemcpyHostToDevice, st), "rl_run_host: upload start");
+	}
+	const int status = iane_gb_rl_run(plan, &ov, &ev, iterations, epsilon, init, base, plan->scratch_bytes, nullptr,
+		stream);
+	if (status) return status;
+	IANE_GB_CUDA(cudaMemcpy2DAsync(host_estimate, nx * 4, d_est, pitch * 4, nx * 4, static_cast<size_t>(ny) * nz,
+		cudaMemcpyDeviceToHost, st), "rl_run_host: download");
+	IANE_GB_CUDA(cudaStreamSynchronize(st), "rl_run_host: wait");
+	return IANE_GB_OK;
+}
+
+}  // extern "C"

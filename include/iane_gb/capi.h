@@ -1,0 +1,175 @@
+/*
+ * iane_gb C ABI: GB300 (sm_103a) kernels for IANE's N-dimensional convolution and the
+ * Richardson-Lucy (RL) deconvolution iteration built on it.
+ *
+ * Every entry point takes plain pointers, sizes and a CUDA stream handle (passed as
+ * `void*`, a `cudaStream_t`); no C++ or PyTorch type crosses this boundary. All image
+ * pointers are device pointers borrowed for the duration of the stream-ordered work;
+ * the caller keeps the storage alive until the stream has completed it, exactly as
+ * IANE requires for CUDA views (include/iane/algorithms/convolution.hpp:88-89 of the
+ * reference: "Keep all view storage valid until completion").
+ *
+ * Functions return IANE_GB_OK (0) or a negative iane_gb_status. The message of the
+ * last failure on the calling thread is available through iane_gb_last_error(). No
+ * entry point traps on the device; device-side waits are bounded and reported as
+ * IANE_GB_DEVICE_TIMEOUT.
+ *
+ * Layout: a view is IANE's strided view (include/iane/view/const_device_image_view.hpp:8-50,
+ * include/iane/math/offset.hpp:11-21): a base pointer to element (0,...,0), a rank
+ * (1..3), extents with axis 0 fastest, and byte strides per axis. Strides may pad rows
+ * and planes and may describe crops of larger allocations; the view extent is the
+ * sampling boundary even for crops (include/iane/locator/image_locator.hpp:18-21).
+ */
+#ifndef IANE_GB_CAPI_H
+#define IANE_GB_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IANE_GB_ABI_VERSION 1
+#define IANE_GB_MAX_RANK 3
+
+/* Element types. f64 is accepted for the exact-accumulation path only. */
+typedef enum iane_gb_dtype {
+	IANE_GB_U8 = 1,
+	IANE_GB_U16 = 2,
+	IANE_GB_I16 = 3,
+	IANE_GB_I32 = 4,
+	IANE_GB_F32 = 5,
+	IANE_GB_F64 = 6,
+	IANE_GB_BF16 = 7
+} iane_gb_dtype;
+
+/* Boundary rules. clamp and zero are the reference's border_mode
+ * (include/iane/locator/image_locator.hpp:14); mirror is an addition: half-sample
+ * symmetric reflection (... c b a | a b c d | d c b ...), repeated with period 2n
+ * for kernels wider than the image. */
+typedef enum iane_gb_border {
+	IANE_GB_BORDER_CLAMP = 0,
+	IANE_GB_BORDER_ZERO = 1,
+	IANE_GB_BORDER_MIRROR = 2
+} iane_gb_border;
+
+typedef enum iane_gb_status {
+	IANE_GB_OK = 0,
+	IANE_GB_INVALID_ARGUMENT = -1, /* the reference throws std::invalid_argument */
+	IANE_GB_UNSUPPORTED = -2,      /* a type, rank or layout this library does not take */
+	IANE_GB_CUDA_ERROR = -3,       /* the reference throws std::runtime_error (check_cuda) */
+	IANE_GB_DEVICE_TIMEOUT = -4,   /* a bounded device wait gave up */
+	IANE_GB_OUT_OF_MEMORY = -5,
+	IANE_GB_LENGTH_ERROR = -6      /* scratch smaller than required (std::length_error) */
+} iane_gb_status;
+
+/* Convolution flags. */
+#define IANE_GB_ACC_FAST 0u  /* FP32 accumulation for float kernels, int64 for integer pairs */
+#define IANE_GB_ACC_EXACT 1u /* FP64 fma in kernel raster order: bit-identical to the reference */
+
+typedef struct iane_gb_view {
+	void* ptr;              /* device address of element (0,...,0) */
+	int32_t dtype;          /* iane_gb_dtype */
+	int32_t rank;           /* 1..IANE_GB_MAX_RANK */
+	int32_t extent[3];      /* axis 0 fastest; unused axes ignored */
+	int32_t reserved;
+	int64_t stride[3];      /* byte strides; unused axes ignored */
+} iane_gb_view;
+
+/* Library identification. */
+int iane_gb_abi_version(void);
+
+/* Copy the calling thread's last error message into buf (NUL-terminated, truncated to
+ * size). Returns the full message length. */
+size_t iane_gb_last_error(char* buf, size_t size);
+
+/* Read and clear the current device's status word after waiting for `stream`. Returns
+ * IANE_GB_DEVICE_TIMEOUT if a bounded device-side wait of an earlier launch gave up. */
+int iane_gb_device_status(void* stream);
+
+/*
+ * Direct N-D convolution. Replaces iane::convolve for CUDA memory views
+ * (reference include/iane/algorithms/convolution.hpp:97-117, with the extent check of
+ * include/iane/algorithms/transform.hpp:51-63):
+ *
+ *   dst[p] = sum_q kernel[q] * sample(src, p + size/2 - q)
+ *
+ * with the kernel flipped (true convolution), kernel extents positive and odd, dst of
+ * the same extents as src and disjoint from both inputs. The kernel is a device view of
+ * the same rank. Results follow the reference's casts (convolution.hpp:51-75):
+ * u8 rounds half up and saturates; other integers saturate and map NaN to 0.
+ * Supported: src u8/u16/i16/i32/f32/bf16/f64, kernel i32/f32/f64, dst u8/u16/i16/i32/f32/f64.
+ */
+int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel,
+	const iane_gb_view* dst, int border, unsigned flags, void* stream);
+
+/*
+ * Separable convolution: the convolution with the outer-product kernel
+ * K[a,b,c] = taps[0][a] * taps[1][b] * taps[2][c], evaluated as one fused pass (axis 0,
+ * then 1, then 2, intermediate rows kept on chip). taps[i] is a 1-D f32 device view of
+ * odd length for axis i; there are exactly src->rank of them. src and dst are f32.
+ * No counterpart in the reference (it has no separable path); its result equals
+ * iane::convolve with the outer-product kernel, and equals successive convolve calls
+ * with unit-extent kernels up to FP32 rounding.
+ */
+int iane_gb_convolve_separable(const iane_gb_view* src, const iane_gb_view* const* taps,
+	const iane_gb_view* dst, int border, void* stream);
+
+/*
+ * Richardson-Lucy deconvolution as an IANE prepared algorithm
+ * (reference include/iane/execution/prepared.hpp:120-146 for the prepare/run/scratch
+ * protocol; examples/rl_deconvolution/main.cu:51-81 for the iteration):
+ *
+ *   sensitivity = convolve(1, adjoint, zero border)           (once, at prepare)
+ *   estimate    = init(observed)
+ *   repeat:  ratio    = observed / max(convolve(estimate, psf, zero), eps)
+ *            estimate = estimate * (sens > 0 ? convolve(ratio, adjoint, zero) / max(sens, eps) : 0)
+ *
+ * adjoint = the PSF reversed along every axis. Each iteration is two fused passes over
+ * HBM. The PSF is an f32 device view of odd extents with the image's rank; it is used as
+ * given (callers normalise it, as examples/common/deconvolution.hpp:10-30 does).
+ */
+typedef struct iane_gb_rl_plan iane_gb_rl_plan;
+
+#define IANE_GB_RL_INIT_OBSERVED 0 /* max(observed, eps): the reference example's start */
+#define IANE_GB_RL_INIT_MEAN 1     /* flat start at max(mean(observed), eps) */
+#define IANE_GB_RL_INIT_GIVEN 2    /* start from the values already in the estimate view */
+
+/* Prepare for images of `extent` (rank 1..3). Copies the PSF, builds its adjoint and the
+ * exact boundary-sensitivity table. Blocks until the copies are done. */
+int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
+	void* stream, iane_gb_rl_plan** plan);
+
+/* Scratch bytes iane_gb_rl_run needs (ratio image, statistics), 256-byte aligned. */
+size_t iane_gb_rl_scratch_bytes(const iane_gb_rl_plan* plan);
+
+/* Run `iterations` RL iterations. observed: f32 or u8; estimate: f32 (the result,
+ * packed or strided) or u8 (converted at the end with the reference's to_gray8,
+ * examples/common/deconvolution.hpp:43-55; then scratch also holds the float estimate).
+ * If stats is non-NULL it is a DEVICE array of 2*iterations doubles that receives, per
+ * iteration, the flux sum(estimate) and the relative L2 change
+ * ||e_new - e_old|| / ||e_old||, from FP32 Kahan partials combined in FP64. */
+int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed,
+	const iane_gb_view* estimate, int iterations, float epsilon, int init,
+	void* scratch, size_t scratch_bytes, double* stats, void* stream);
+
+/* Bytes of device scratch iane_gb_rl_run_host needs: run scratch plus packed device
+ * copies of the observed and estimate images. */
+size_t iane_gb_rl_host_scratch_bytes(const iane_gb_rl_plan* plan, int observed_dtype);
+
+/* End-to-end run from packed HOST images (the reference's run_prepared_on staging,
+ * include/iane/execution/run_on.hpp:86-178): upload observed, run, download the f32
+ * estimate, then wait for the stream. Host buffers should be pinned for full speed. */
+int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int observed_dtype,
+	float* host_estimate, int iterations, float epsilon, int init,
+	void* scratch, size_t scratch_bytes, void* stream);
+
+/* Release a plan (after the stream has finished work that uses it). NULL is accepted. */
+int iane_gb_rl_destroy(iane_gb_rl_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IANE_GB_CAPI_H */

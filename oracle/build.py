@@ -1,0 +1,73 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+* ``oracle/liboracle.so`` -- the C restatement in ``iane_oracle.c`` (gcc, pthreads).
+  Built everywhere, including the GPU host.
+* ``oracle/_ref/libiane_ref.so`` -- ``ref_shim.cpp`` compiled against the reference's own
+  headers, read in place from the reference checkout (``IANE_REFERENCE`` or
+  ``/root/reference``). Built only where that checkout exists; never copied.
+
+Run as ``python oracle/build.py``.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_DIR = HERE / "_ref"
+ORACLE_LIB = HERE / "liboracle.so"
+REF_LIB = REF_DIR / "libiane_ref.so"
+
+
+def reference_root() -> Path | None:
+    root = Path(os.environ.get("IANE_REFERENCE", "/root/reference"))
+    return root if (root / "include" / "iane" / "algorithms" / "convolution.hpp").is_file() else None
+
+
+def _stale(target: Path, sources: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    mtime = target.stat().st_mtime
+    return any(s.stat().st_mtime > mtime for s in sources)
+
+
+def build_oracle(force: bool = False) -> Path:
+    src = HERE / "iane_oracle.c"
+    header = HERE.parent / "include" / "iane_gb" / "capi.h"
+    if force or _stale(ORACLE_LIB, [src, header]):
+        tmp = ORACLE_LIB.with_suffix(".so.tmp")
+        subprocess.check_call([
+            "gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
+            str(src), "-o", str(tmp), "-lm",
+        ])
+        os.replace(tmp, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def build_reference(force: bool = False) -> Path | None:
+    root = reference_root()
+    if root is None:
+        return None
+    src = HERE / "ref_shim.cpp"
+    header = HERE.parent / "include" / "iane_gb" / "capi.h"
+    if force or _stale(REF_LIB, [src, header]):
+        REF_DIR.mkdir(exist_ok=True)
+        tmp = REF_LIB.with_suffix(".so.tmp")
+        subprocess.check_call([
+            "g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
+            "-I", str(root / "include"), str(src), "-o", str(tmp),
+        ])
+        os.replace(tmp, REF_LIB)
+    return REF_LIB
+
+
+def main() -> int:
+    print(build_oracle(force="--force" in sys.argv))
+    print(build_reference(force="--force" in sys.argv) or "reference checkout absent: oracle/_ref not built")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -1,0 +1,48 @@
+"""Access to the golden vectors (tests/golden/golden.npz, made by make_golden.py)."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "golden.npz"
+_data = None
+
+
+def data():
+    global _data
+    if _data is None:
+        _data = dict(np.load(GOLDEN))
+    return _data
+
+
+def conv_cases():
+    d = data()
+    names = sorted({k.split("__")[0] for k in d if k.endswith("__border")})
+    return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"], str(d[f"{n}__border"])) for n in names]
+
+
+def mirror_cases():
+    d = data()
+    return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"]) for n in ("mirror_2d", "mirror_3d")]
+
+
+def rl_cases():
+    d = data()
+    out = []
+    for name, init, iters in (("rl_3d_init0", 0, 8), ("rl_3d_init1", 1, 8), ("rl_2d", 0, 12)):
+        out.append((name, d[f"{name}__obs"], d[f"{name}__psf"], d[f"{name}__out"], init, iters))
+    return out
+
+
+def bench_pattern(width, height):
+    """The reference benchmark's image and kernel (benchmarks/convolution.cu:88-96)."""
+    i = np.arange(width * height, dtype=np.int64)
+    image = (((i * 19) ^ (i // width)) & 0xFF).astype(np.uint8).reshape(height, width)
+    k = np.arange(81, dtype=np.int64)
+    kernel = (((k * 3) % 7 - 2) / 64.0).astype(np.float32).reshape(9, 9)
+    return image, kernel
+
+
+def bench_sha256() -> str:
+    return str(data()["bench_u8_2560x1920__sha256"])

@@ -1,0 +1,140 @@
+"""The CPU oracle is pinned: it reproduces the reference's known answers, the golden
+vectors made by the reference, and (where the reference is built here) the live reference
+on random inputs, bit for bit."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_cases import bench_pattern, conv_cases, mirror_cases, rl_cases
+
+
+def test_known_answer_1d_flip_zero_border():
+    # test/unit/algorithms/test_convolution.cpp:10-23 of the reference
+    out = np.zeros(3, np.int32)
+    oracle.convolve(np.array([1, 2, 3], np.int32), np.array([1, 0, 0], np.int32), out, "zero")
+    assert out.tolist() == [2, 3, 0]
+
+
+@pytest.mark.parametrize("border,expected", [("clamp", [20, 20, 120, 120]), ("zero", [20, 0, 120, 0])])
+def test_known_answer_crop_boundary(border, expected):
+    # test/unit/algorithms/test_convolution.cpp:25-51: the crop's extent is the boundary
+    source = np.array([[10 * x + 100 * y for x in range(4)] for y in range(2)], np.uint8)
+    crop = source[:, 1:3]
+    out = np.zeros((2, 2), np.uint8)
+    oracle.convolve(crop, np.array([[1, 0, 0]], np.float32), out, border)
+    assert out.ravel().tolist() == expected
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_known_answer_nd_last_axis(dim):
+    # test/unit/algorithms/convolution_cases.hpp:12-34 (channel 0 of its pixel element):
+    # 3^N image of i+1, kernel {2,-1,0} along the last axis, zero border.
+    shape = (3,) * dim
+    src = (np.arange(3 ** dim, dtype=np.int32) + 1).reshape(shape)
+    kshape = (3,) + (1,) * (dim - 1)
+    kernel = np.array([2, -1, 0], np.int32).reshape(kshape)
+    out = np.zeros(shape, np.int32)
+    oracle.convolve(src, kernel, out, "zero")
+    plane = 3 ** (dim - 1)
+    flat = src.ravel()
+    layer = np.arange(flat.size) // plane
+    nxt = np.where(layer == 2, 0, flat + plane)
+    assert np.array_equal(out.ravel(), 2 * nxt - flat)
+
+
+@pytest.mark.parametrize("case", conv_cases(), ids=lambda c: c[0])
+def test_oracle_matches_golden_convolution(case):
+    name, src, kernel, expected, border = case
+    out = np.zeros(expected.shape, expected.dtype)
+    oracle.convolve(src, kernel, out, border)
+    assert np.array_equal(out, expected), name
+
+
+@pytest.mark.parametrize("case", mirror_cases(), ids=lambda c: c[0])
+def test_oracle_mirror_matches_padded_reference(case):
+    name, src, kernel, expected = case
+    out = np.zeros(expected.shape, np.float32)
+    oracle.convolve(src, kernel, out, "mirror")
+    assert np.array_equal(out, expected), name
+
+
+@pytest.mark.parametrize("case", rl_cases(), ids=lambda c: c[0])
+def test_oracle_matches_golden_rl(case):
+    name, obs, psf, expected, init, iters = case
+    est = oracle.rl(obs, psf, iters, 1e-6, init=init)
+    assert np.array_equal(est, expected), name
+
+
+def test_separable_oracle_equals_sequential_unit_kernels():
+    rng = np.random.default_rng(5)
+    src = rng.random((5, 8, 9), dtype=np.float32)
+    taps = [rng.random(n, dtype=np.float32) for n in (5, 3, 3)]
+    out = np.zeros_like(src)
+    oracle.convolve_separable(src, taps, out, "mirror")
+    a = src
+    for axis, t in enumerate(taps):
+        shape = [1, 1, 1]
+        shape[2 - axis] = t.size
+        nxt = np.zeros_like(src)
+        oracle.convolve(a, t.reshape(shape), nxt, "mirror")
+        a = nxt
+    assert np.array_equal(out, a)
+
+
+def test_benchmark_pattern_small_exact_in_fp32_accumulation():
+    # The benchmark kernel is k/64: every partial sum is exact in FP32 as well as FP64,
+    # which is why GPU FP32 accumulation reproduces the reference's bytes bit-exactly.
+    image, kernel = bench_pattern(64, 48)
+    out = np.zeros(image.shape, np.uint8)
+    oracle.convolve(image, kernel, out, "clamp")
+    assert out.dtype == np.uint8 and out.shape == (48, 64)
+
+
+def test_sensitivity_interior_is_kernel_sum():
+    psf = np.random.default_rng(1).random((3, 5, 7), dtype=np.float32)
+    s = oracle.sensitivity(psf, (9, 10, 11))
+    assert abs(float(s[4, 5, 5]) - float(psf.astype(np.float64).sum())) < 1e-5
+    assert float(s[0, 0, 0]) < float(s[4, 5, 5])
+
+
+reference = pytest.mark.skipif(not oracle.reference_available(), reason="reference checkout not built here")
+
+
+@reference
+@pytest.mark.parametrize("border", ["clamp", "zero"])
+@pytest.mark.parametrize("shape,kshape", [((31,), (7,)), ((12, 17), (5, 3)), ((6, 7, 9), (3, 5, 7)), ((3, 4, 5), (7, 9, 11))])
+def test_oracle_matches_live_reference_f32(border, shape, kshape):
+    rng = np.random.default_rng(sum(shape) + len(border))
+    src = rng.standard_normal(shape).astype(np.float32)
+    kernel = rng.standard_normal(kshape).astype(np.float32)
+    a, b = np.zeros_like(src), np.zeros_like(src)
+    oracle.convolve(src, kernel, a, border)
+    oracle.convolve(src, kernel, b, border, use_reference=True)
+    assert np.array_equal(a, b)
+
+
+@reference
+def test_oracle_matches_live_reference_strided_views():
+    rng = np.random.default_rng(3)
+    big = rng.random((9, 20, 24), dtype=np.float32)
+    src = big[1:8, 2:17:2, 3:21]
+    kernel = rng.random((3, 3, 5), dtype=np.float32)
+    a = np.zeros((7, 8, 18), np.float32)
+    b = np.zeros((7, 8, 40), np.float32)[:, :, ::2][:, :, :18]
+    oracle.convolve(src, kernel, a, "clamp")
+    oracle.convolve(src, kernel, b, "clamp", use_reference=True)
+    assert np.array_equal(a, b)
+
+
+@reference
+def test_oracle_rl_matches_live_reference_with_u8_like_data():
+    rng = np.random.default_rng(11)
+    obs = rng.integers(0, 256, (7, 9, 12)).astype(np.float32)
+    psf = rng.random((3, 3, 5), dtype=np.float32)
+    psf /= psf.sum()
+    for init in (0, 1):
+        a = oracle.rl(obs, psf, 6, 1e-6, init=init)
+        b = oracle.rl(obs, psf, 6, 1e-6, init=init, use_reference=True)
+        assert np.array_equal(a, b)
