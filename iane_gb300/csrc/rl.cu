@@ -420,9 +420,11 @@ int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const ia
 	int* dstatus = device_status_ptr();
 	if (!dstatus) return IANE_GB_CUDA_ERROR;
 	const int kx = plan->k[0];
+	// Tile shape of the launches below: (1, 1) warps for small images, else (2, 2).
 	const int wx = plan->small_tiles ? 1 : 2;
+	const int wy = wx;
 	const int box_w = tile_pitch(kx, wx);
-	const int box_h = 32 * wx + 2 * (plan->k[1] / 2);
+	const int box_h = 32 * wy + 2 * (plan->k[1] / 2);
 	CUtensorMap map_est{}, map_ratio{};
 	status = encode_tensor_map_f32(&map_est, e_work, nx, ny, nz, pitch * 4, plane * 4, box_w, box_h);
 	if (status) return status;
