@@ -130,6 +130,7 @@ int launch_conv_separable(const DevView& src, const DevView* taps, const DevView
 	SepArgs a{};
 	a.src = src;
 	a.dst = dst;
+	a.border = border;
 	for (int i = 0; i < 3; ++i) {
 		a.k[i] = taps[i].ext[0];
 		a.taps[i] = taps[i].ptr;

@@ -85,9 +85,11 @@ def test_golden_fast_mode(cuda, case):
     elif expected.dtype in (np.float32, np.float64):
         check_fp32(out, expected, src, kernel, border)
     else:
-        # float data into an integer destination: the FP32 sum may round across a
-        # boundary of the cast, so allow one unit; exact mode is bit-identical (above)
-        assert np.all(np.abs(out.astype(np.int64) - expected.astype(np.int64)) <= 1), name
+        # float data into an integer destination: the FP32 sum may differ by its rounding
+        # error and then round across a boundary of the cast, so allow one unit beyond the
+        # FP32 bound; exact mode is bit-identical (above)
+        slack = 1.0 + FP32_TOL * magnitude(src, kernel, border)
+        assert np.all(np.abs(out.astype(np.float64) - expected.astype(np.float64)) <= slack), name
 
 
 @pytest.mark.parametrize("case", mirror_cases(), ids=lambda c: c[0])
