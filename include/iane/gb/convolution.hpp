@@ -1,0 +1,228 @@
+// Drop-in GB300 dispatch for IANE's convolution and a prepared Richardson-Lucy algorithm.
+//
+// Include this header after (or instead of) <iane/algorithms/convolution.hpp> and link
+// libiane_gb300.so. Existing call sites
+//
+//     iane::convolve(src, kernel, dst, {.border = iane::border_mode::zero}, iane::cuda_policy{stream});
+//
+// on CUDA memory views (const_device_image_view / device_image_view) of u8, u16, i16, i32,
+// f32 or f64 elements, rank 1 to 3, then resolve to the overload below, which carries the
+// reference template's constraints (include/iane/algorithms/convolution.hpp:91-96) plus
+// native_view on all three views and therefore wins overload resolution as the more
+// constrained candidate. Texture views, procedural views, custom element types and host
+// views keep resolving to the reference's generic template. The call is asynchronous on
+// the policy's stream, returns an execution handle whose wait() synchronises it, and
+// reports errors with the reference's exception types: std::invalid_argument for kernel
+// extents that are not positive and odd or for mismatched image extents, std::runtime_error
+// for CUDA failures (include/iane/execution/context.hpp:36-41).
+//
+// iane::gb::richardson_lucy plugs the RL loop of examples/rl_deconvolution/main.cu:51-81
+// into the prepared-algorithm protocol (include/iane/execution/prepared.hpp:120-146):
+//
+//     auto exec = iane::make_execution_context(iane::cuda_policy{stream});
+//     auto op = exec.prepare(iane::gb::richardson_lucy{psf, 50, 1e-6f}, observed, estimate);
+//     exec.run(op, observed, estimate).wait();
+#pragma once
+
+#include <iane/algorithms/convolution.hpp>
+#include <iane/execution/context.hpp>
+#include <iane/execution/prepared.hpp>
+#include <iane_gb/capi.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+
+namespace iane::gb {
+
+/// Completion handle of a GB300 launch; a cuda_execution for all uses.
+struct execution : cuda_execution {};
+
+/// Accumulation for the convolution overload: fast (FP32, or int64 for integer pairs) or
+/// exact (FP64 in the reference's tap order, bit-identical to the reference).
+enum class accumulation { fast, exact };
+
+/// Accumulation used by iane::convolve on native views in the calling thread.
+inline accumulation& thread_accumulation()
+{
+	thread_local accumulation mode = accumulation::fast;
+	return mode;
+}
+
+namespace detail {
+
+template<class T> inline constexpr int dtype_code = 0;
+template<> inline constexpr int dtype_code<std::uint8_t> = IANE_GB_U8;
+template<> inline constexpr int dtype_code<std::uint16_t> = IANE_GB_U16;
+template<> inline constexpr int dtype_code<std::int16_t> = IANE_GB_I16;
+template<> inline constexpr int dtype_code<std::int32_t> = IANE_GB_I32;
+template<> inline constexpr int dtype_code<float> = IANE_GB_F32;
+template<> inline constexpr int dtype_code<double> = IANE_GB_F64;
+
+/// A CUDA memory view whose element type and rank the GB300 kernels take.
+template<class TView>
+concept native_view = concepts::DeviceView<TView> && concepts::MemoryView<TView> &&
+	(TView::dimension >= 1) && (TView::dimension <= IANE_GB_MAX_RANK) &&
+	(dtype_code<std::remove_cv_t<typename TView::value_type>> != 0);
+
+template<class TView>
+iane_gb_view to_view(const TView& aView)
+{
+	iane_gb_view v{};
+	v.ptr = const_cast<void*>(static_cast<const void*>(aView.pointer()));
+	v.dtype = dtype_code<std::remove_cv_t<typename TView::value_type>>;
+	v.rank = TView::dimension;
+	const auto size = aView.dimensions();
+	const auto strides = aView.strides();
+	for (int i = 0; i < TView::dimension; ++i) {
+		v.extent[i] = math::detail::axis(size, i);
+		v.stride[i] = math::detail::axis(strides, i);
+	}
+	return v;
+}
+
+inline std::string last_error()
+{
+	char buffer[512];
+	iane_gb_last_error(buffer, sizeof buffer);
+	return buffer;
+}
+
+/// Map a C-ABI status to the exception the reference throws in the same situation.
+inline void check(int aStatus)
+{
+	switch (aStatus) {
+	case IANE_GB_OK: return;
+	case IANE_GB_INVALID_ARGUMENT: throw std::invalid_argument(last_error());
+	case IANE_GB_LENGTH_ERROR: throw std::length_error(last_error());
+	case IANE_GB_OUT_OF_MEMORY: throw std::bad_alloc();
+	default: throw std::runtime_error(last_error());
+	}
+}
+
+inline int border_code(border_mode aBorder)
+{
+	return aBorder == border_mode::zero ? IANE_GB_BORDER_ZERO : IANE_GB_BORDER_CLAMP;
+}
+
+} // namespace detail
+
+/// Start value of a Richardson-Lucy run.
+enum class rl_start {
+	observed = IANE_GB_RL_INIT_OBSERVED, ///< max(observed, eps), as examples/rl_deconvolution
+	mean = IANE_GB_RL_INIT_MEAN,         ///< flat start at max(mean(observed), eps)
+	given = IANE_GB_RL_INIT_GIVEN        ///< the estimate view's current contents
+};
+
+/// Prepared state: owns the plan (PSF copies, adjoint, edge-sensitivity table).
+class richardson_lucy_state {
+public:
+	richardson_lucy_state(iane_gb_rl_plan* aPlan, int aIterations, float aEpsilon, rl_start aStart)
+		: mPlan(aPlan), mIterations(aIterations), mEpsilon(aEpsilon), mStart(aStart) {}
+
+	std::size_t scratch_bytes() const { return iane_gb_rl_scratch_bytes(mPlan.get()); }
+
+	template<class TSrc, class TDst>
+	requires (detail::native_view<TSrc> && detail::native_view<TDst> && concepts::MatchingViewRank<TSrc, TDst>)
+	execution run(TSrc aSource, TDst aDestination, iane::detail::scratch_space<cuda_policy>& aScratch,
+		cuda_policy aPolicy)
+	{
+		const auto bytes = scratch_bytes();
+		void* scratch = aScratch.bytes(bytes, alignof(std::max_align_t));
+		const auto src = detail::to_view(aSource);
+		const auto dst = detail::to_view(aDestination);
+		detail::check(iane_gb_rl_run(mPlan.get(), &src, &dst, mIterations, mEpsilon, static_cast<int>(mStart),
+			scratch, bytes, nullptr, aPolicy.stream));
+		return {{aPolicy.stream}};
+	}
+
+private:
+	struct plan_deleter {
+		void operator()(iane_gb_rl_plan* aPlan) const noexcept { iane_gb_rl_destroy(aPlan); }
+	};
+	std::unique_ptr<iane_gb_rl_plan, plan_deleter> mPlan;
+	int mIterations;
+	float mEpsilon;
+	rl_start mStart;
+};
+
+/**
+ * @brief Richardson-Lucy deconvolution as a prepared algorithm for CUDA contexts.
+ * @tparam TPsf An f32 CUDA memory view of odd extents with the image rank; normalise it to
+ * sum 1 beforehand, as examples/common/deconvolution.hpp:10-30 does.
+ *
+ * Each iteration is two fused passes: convolve(estimate, psf) with the guarded ratio
+ * observed / max(pred, eps) in its epilogue, then convolve(ratio, adjoint) with the edge
+ * correction and the multiplicative update in its epilogue (zero border throughout).
+ */
+template<class TPsf>
+requires detail::native_view<TPsf>
+struct richardson_lucy {
+	TPsf psf;
+	int iterations = 20;
+	float epsilon = 1e-6f;
+	rl_start start = rl_start::observed;
+
+	template<class TSrc, class TDst>
+	requires (detail::native_view<TSrc> && detail::native_view<TDst> && concepts::MatchingViewRank<TSrc, TDst>)
+	richardson_lucy_state prepare(TSrc aSource, TDst aDestination, cuda_policy aPolicy) const
+	{
+		const auto psf_view = detail::to_view(psf);
+		const auto size = aSource.dimensions();
+		const auto out = aDestination.dimensions();
+		std::int32_t extent[3] = {1, 1, 1};
+		for (int i = 0; i < TSrc::dimension; ++i) {
+			extent[i] = math::detail::axis(size, i);
+			if (math::detail::axis(out, i) != extent[i]) {
+				throw std::invalid_argument("Source and destination require matching nonnegative dimensions");
+			}
+		}
+		if (iterations < 0 || !(epsilon > 0.0f)) {
+			throw std::invalid_argument("Iterations and finite epsilon must be positive");
+		}
+		iane_gb_rl_plan* plan = nullptr;
+		detail::check(iane_gb_rl_prepare(&psf_view, TSrc::dimension, extent, aPolicy.stream, &plan));
+		return richardson_lucy_state(plan, iterations, epsilon, start);
+	}
+};
+
+template<class TPsf>
+richardson_lucy(TPsf, int, float) -> richardson_lucy<TPsf>;
+template<class TPsf>
+richardson_lucy(TPsf, int, float, rl_start) -> richardson_lucy<TPsf>;
+
+} // namespace iane::gb
+
+namespace iane {
+
+/**
+ * @brief GB300 convolution for CUDA memory views (see the file comment).
+ *
+ * Same contract as the reference's iane::convolve. Accumulation follows
+ * iane::gb::thread_accumulation(): FP32 by default, FP64 in the reference's order when set
+ * to accumulation::exact.
+ */
+template<class TSrc, class TKernel, class TDst>
+requires (concepts::TransformViews<TSrc, TDst> &&
+	concepts::ReadableView<TKernel> &&
+	concepts::MatchingViewRank<TKernel, TSrc> &&
+	concepts::SameViewBackend<TKernel, TSrc> &&
+	concepts::ConvolutionElements<typename TSrc::value_type, typename TKernel::value_type,
+		typename TDst::value_type> &&
+	gb::detail::native_view<TSrc> && gb::detail::native_view<TKernel> && gb::detail::native_view<TDst>)
+gb::execution convolve(TSrc aSource, TKernel aKernel, TDst aDestination,
+	convolution_options aOptions = {}, view_policy<TDst> aPolicy = {})
+{
+	const auto src = gb::detail::to_view(aSource);
+	const auto kernel = gb::detail::to_view(aKernel);
+	const auto dst = gb::detail::to_view(aDestination);
+	const unsigned flags = gb::thread_accumulation() == gb::accumulation::exact ? IANE_GB_ACC_EXACT : IANE_GB_ACC_FAST;
+	gb::detail::check(iane_gb_convolve(&src, &kernel, &dst, gb::detail::border_code(aOptions.border), flags,
+		aPolicy.stream));
+	return {{aPolicy.stream}};
+}
+
+} // namespace iane

@@ -1,0 +1,97 @@
+// Compile-and-run check of the C++ drop-in (include/iane/gb/convolution.hpp) against the
+// reference's own headers: overload selection, exception mapping, and -- where a GPU is
+// present -- a convolution and a prepared Richardson-Lucy run through iane's own API.
+#include <iane/algorithms/convolution.hpp>
+#include <iane/algorithms/copy.hpp>
+#include <iane/image/image.hpp>
+#include <iane/resource/cuda/resource_cuda.hpp>
+#include <iane/resource/host/resource_host.hpp>
+#include <iane/gb/convolution.hpp>
+
+#include <cmath>
+#include <cstdio>
+#include <stdexcept>
+#include <type_traits>
+#include <utility>
+
+namespace {
+
+using dev_src = iane::const_device_image_view<float, 3>;
+using dev_dst = iane::device_image_view<float, 3>;
+using dev_src8 = iane::const_device_image_view<std::uint8_t, 2>;
+using dev_dst8 = iane::device_image_view<std::uint8_t, 2>;
+using dev_k2 = iane::const_device_image_view<float, 2>;
+using host_src = iane::const_host_image_view<float, 2>;
+using host_dst = iane::host_image_view<float, 2>;
+
+// CUDA memory views of supported types resolve to the GB300 overload ...
+static_assert(std::is_same_v<decltype(iane::convolve(std::declval<dev_src>(), std::declval<dev_src>(),
+	std::declval<dev_dst>())), iane::gb::execution>);
+static_assert(std::is_same_v<decltype(iane::convolve(std::declval<dev_src8>(), std::declval<dev_k2>(),
+	std::declval<dev_dst8>(), iane::convolution_options{}, iane::cuda_policy{})), iane::gb::execution>);
+// ... host views keep the reference's template.
+static_assert(!std::is_same_v<decltype(iane::convolve(std::declval<host_src>(), std::declval<host_src>(),
+	std::declval<host_dst>())), iane::gb::execution>);
+
+int failures = 0;
+
+template<class F>
+void expect_invalid_argument(const char* what, F&& f)
+{
+	try {
+		f();
+		std::printf("FAIL %s: no exception\n", what);
+		++failures;
+	} catch (const std::invalid_argument&) {
+		std::printf("ok   %s\n", what);
+	} catch (const std::exception& e) {
+		std::printf("FAIL %s: wrong exception %s\n", what, e.what());
+		++failures;
+	}
+}
+
+} // namespace
+
+int main()
+{
+	// Argument errors are detected before any CUDA call, so they need no device.
+	float storage[64] = {};
+	using v3 = iane::math::vec3i;
+	const dev_src src(storage, v3{4, 4, 4}, v3{4, 16, 64});
+	const dev_dst dst(storage, v3{4, 4, 4}, v3{4, 16, 64});
+	const dev_src even(storage, v3{2, 3, 3}, v3{4, 8, 24});
+	const dev_dst smaller(storage, v3{4, 4, 3}, v3{4, 16, 64});
+	expect_invalid_argument("even kernel extent", [&] { iane::convolve(src, even, dst); });
+	expect_invalid_argument("mismatched extents", [&] { iane::convolve(src, src, smaller); });
+
+	int devices = 0;
+	if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) {
+		std::printf("no CUDA device: GPU part skipped\n");
+		return failures == 0 ? 0 : 1;
+	}
+	// GPU part: 3-D convolution against the reference's CPU convolution, then prepared RL.
+	iane::host_image<float, 3> h_src(20, 18, 9), h_ref(20, 18, 9), h_out(20, 18, 9);
+	iane::host_image<float, 3> h_k(5, 3, 3);
+	for (int i = 0; i < 20 * 18 * 9; ++i) h_src.pointer()[i] = static_cast<float>((i * 37) % 101) / 7.0f;
+	for (int i = 0; i < 45; ++i) h_k.pointer()[i] = static_cast<float>(i % 7 + 1) / 100.0f;
+	iane::convolve(h_src.const_view(), h_k.const_view(), h_ref.view(), {iane::border_mode::zero});
+	iane::device_image<float, 3> d_src(20, 18, 9), d_out(20, 18, 9), d_k(5, 3, 3);
+	iane::copy(h_src.const_view(), d_src.view()).wait();
+	iane::copy(h_k.const_view(), d_k.view()).wait();
+	iane::gb::thread_accumulation() = iane::gb::accumulation::exact;
+	iane::convolve(d_src.const_view(), d_k.const_view(), d_out.view(), {iane::border_mode::zero}).wait();
+	iane::copy(d_out.const_view(), h_out.view()).wait();
+	for (int i = 0; i < 20 * 18 * 9; ++i) {
+		if (h_out.pointer()[i] != h_ref.pointer()[i]) {
+			std::printf("FAIL exact convolution differs at %d\n", i);
+			return 1;
+		}
+	}
+	std::printf("ok   exact convolution matches the reference\n");
+	auto exec = iane::make_execution_context(iane::cuda_policy{});
+	auto op = exec.prepare(iane::gb::richardson_lucy{d_k.const_view(), 5, 1e-6f, iane::gb::rl_start::mean},
+		d_src.const_view(), d_out.view());
+	exec.run(op, d_src.const_view(), d_out.view()).wait();
+	std::printf("ok   prepared Richardson-Lucy ran\n");
+	return failures == 0 ? 0 : 1;
+}
