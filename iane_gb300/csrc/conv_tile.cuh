@@ -12,9 +12,10 @@
 //     next plane lands while this one is consumed;
 //   * a lane walks the RY + 2 ry input rows it needs; each row segment (8 + 2 rx floats) is
 //     read once with 128-bit shared loads into registers and feeds every (output row j,
-//     kernel row b) pair that uses it: 8 x KX FMAs per (j, b), issued as packed FP32 FMAs
-//     (__ffma2_rn, two adjacent outputs per instruction) against kernel taps that are read
-//     as warp-uniform broadcasts of duplicated (k, k) pairs;
+//     kernel row b) pair that uses it: 8 x KX FMAs per (j, b) against a kernel row that is
+//     read as a warp-uniform broadcast (packed f32x2 FMAs were measured slower here: half
+//     the taps need operand pairs at odd offsets, and the register moves that build them
+//     cost more issue slots than the packing saves);
 //   * only the current and next kernel planes' taps are held in shared memory, so four
 //     64x64-tile blocks fit per SM.
 // Per kernel plane each output accumulates its ky*kx taps into a plane partial that is
@@ -67,7 +68,7 @@ inline size_t tile_smem_bytes(int ky, int kz)
 {
 	const int H = 32 * WY + 2 * (ky / 2);
 	const size_t plane = (static_cast<size_t>(TileWidth<KX, WX>::P) * H * 4 + 127) & ~size_t(127);
-	const size_t psf = (static_cast<size_t>(ky) * TileGeom<KX>::KXP * 8 + 127) & ~size_t(127);
+	const size_t psf = (static_cast<size_t>(ky) * TileGeom<KX>::KXP * 4 + 127) & ~size_t(127);
 	(void)kz;
 	return 2 * plane + 2 * psf + 16;
 }
@@ -89,9 +90,9 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	const int H = TY + 2 * ry;
 	const int plane_floats = ((P * H + 31) & ~31);
 	float* tiles = reinterpret_cast<float*>(smem_raw);
-	float2* psf_s = reinterpret_cast<float2*>(tiles + 2 * plane_floats); // two planes of (k, k) pairs
-	const int psf_pairs = ((ky * G::KXP + 15) & ~15);
-	uint64_t* bars = reinterpret_cast<uint64_t*>(psf_s + 2 * psf_pairs);
+	float* psf_s = tiles + 2 * plane_floats; // taps of two kernel planes
+	const int psf_floats = ((ky * G::KXP + 31) & ~31);
+	uint64_t* bars = reinterpret_cast<uint64_t*>(psf_s + 2 * psf_floats);
 
 	const int tid = threadIdx.x;
 	const int lane = tid & 31, warp = tid >> 5;
@@ -108,10 +109,10 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	}
 	const int nplanes = qz_hi - qz_lo + 1;
 
-	// Taps of kernel plane qz_lo + p into pair buffer p & 1, each tap duplicated as (k, k).
+	// Taps of kernel plane qz_lo + p into tap buffer p & 1.
 	auto load_taps = [&](int p) {
 		const int qz = qz_lo + p;
-		float2* dst = psf_s + (p & 1) * psf_pairs;
+		float* dst = psf_s + (p & 1) * psf_floats;
 		for (int i = tid; i < ky * G::KXP; i += NT) {
 			const int qx = i % G::KXP, qy = i / G::KXP;
 			float v = 0.0f;
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(32 * WX * WY)
 				v = *reinterpret_cast<const float*>(a.kernel + qx * a.k_stride[0] + qy * a.k_stride[1] +
 					qz * a.k_stride[2]);
 			}
-			dst[i] = make_float2(v, v);
+			dst[i] = v;
 		}
 	};
 	if (nplanes > 0) load_taps(0);
@@ -157,12 +158,11 @@ __global__ void __launch_bounds__(32 * WX * WY)
 		}
 	};
 
-	constexpr int RP = kRX / 2; // output pairs per row
-	float2 acc[kRY][RP];
+	float acc[kRY][kRX];
 #pragma unroll
 	for (int j = 0; j < kRY; ++j)
 #pragma unroll
-		for (int i = 0; i < RP; ++i) acc[j][i] = make_float2(0.0f, 0.0f);
+		for (int i = 0; i < kRX; ++i) acc[j][i] = 0.0f;
 
 	bool ok = true;
 	if (nplanes > 0) issue(0);
@@ -182,49 +182,45 @@ __global__ void __launch_bounds__(32 * WX * WY)
 			__syncthreads();
 		}
 		const float* tile = tiles + (p & 1) * plane_floats + (kRY * ty_b) * P + kRX * tx_b;
-		const float2* kplane = psf_s + (p & 1) * psf_pairs;
-		float2 part[kRY][RP];
+		const float* kplane = psf_s + (p & 1) * psf_floats;
+		float part[kRY][kRX];
 #pragma unroll
 		for (int j = 0; j < kRY; ++j)
 #pragma unroll
-			for (int i = 0; i < RP; ++i) part[j][i] = make_float2(0.0f, 0.0f);
+			for (int i = 0; i < kRX; ++i) part[j][i] = 0.0f;
 
 		const int rows = kRY + 2 * ry;
 #pragma unroll 1
 		for (int r = 0; r < rows; ++r) {
-			// even pairs (seg[2t], seg[2t+1]) straight from the 128-bit loads, odd pairs
-			// (seg[2t+1], seg[2t+2]) rebuilt in registers
-			float2 se[G::SEGN / 2];
-			float2 so[G::SEGN / 2 - 1];
+			float seg[G::SEGN];
 			const float4* srow = reinterpret_cast<const float4*>(tile + r * P);
 #pragma unroll
 			for (int m = 0; m < G::SEGN / 4; ++m) {
 				const float4 v = srow[m];
-				se[2 * m] = make_float2(v.x, v.y);
-				se[2 * m + 1] = make_float2(v.z, v.w);
+				seg[4 * m + 0] = v.x;
+				seg[4 * m + 1] = v.y;
+				seg[4 * m + 2] = v.z;
+				seg[4 * m + 3] = v.w;
 			}
-#pragma unroll
-			for (int t = 0; t < G::SEGN / 2 - 1; ++t) so[t] = make_float2(se[t].y, se[t + 1].x);
 #pragma unroll
 			for (int j = 0; j < kRY; ++j) {
 				const int b = j + 2 * ry - r;
 				if (b >= 0 && b < ky) {
 					const float4* krow = reinterpret_cast<const float4*>(kplane + b * G::KXP);
+					float k[G::KXP];
 #pragma unroll
-					for (int qq = 0; qq < (KX + 1) / 2; ++qq) {
-						const float4 kk = krow[qq];
+					for (int m = 0; m < G::KXP / 4; ++m) {
+						const float4 v = krow[m];
+						k[4 * m + 0] = v.x;
+						k[4 * m + 1] = v.y;
+						k[4 * m + 2] = v.z;
+						k[4 * m + 3] = v.w;
+					}
 #pragma unroll
-						for (int h = 0; h < 2; ++h) {
-							const int q = 2 * qq + h;
-							if (q < KX) {
-								const float2 k2 = h == 0 ? make_float2(kk.x, kk.y) : make_float2(kk.z, kk.w);
+					for (int q = 0; q < KX; ++q) {
 #pragma unroll
-								for (int ip = 0; ip < RP; ++ip) {
-									const int sidx = G::D + 2 * ip + 2 * G::rx - q;
-									const float2 d = (sidx & 1) ? so[sidx >> 1] : se[sidx >> 1];
-									part[j][ip] = __ffma2_rn(d, k2, part[j][ip]);
-								}
-							}
+						for (int i = 0; i < kRX; ++i) {
+							part[j][i] = fmaf(k[q], seg[G::D + i + 2 * G::rx - q], part[j][i]);
 						}
 					}
 				}
@@ -233,7 +229,7 @@ __global__ void __launch_bounds__(32 * WX * WY)
 #pragma unroll
 		for (int j = 0; j < kRY; ++j)
 #pragma unroll
-			for (int i = 0; i < RP; ++i) acc[j][i] = __fadd2_rn(acc[j][i], part[j][i]);
+			for (int i = 0; i < kRX; ++i) acc[j][i] += part[j][i];
 
 		__syncthreads(); // every lane is done with this plane's tile and taps
 		if (p + 2 < nplanes) {
@@ -247,13 +243,7 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	const int yo = y0 + kRY * ty_b;
 #pragma unroll
 	for (int j = 0; j < kRY; ++j) {
-		float v[kRX];
-#pragma unroll
-		for (int i = 0; i < RP; ++i) {
-			v[2 * i] = acc[j][i].x;
-			v[2 * i + 1] = acc[j][i].y;
-		}
-		epi.row(xo, yo + j, z, v);
+		epi.row(xo, yo + j, z, acc[j]);
 	}
 	epi.finish();
 }
