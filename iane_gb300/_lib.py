@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_rl_run_host.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp,
                                       ctypes.c_size_t, vp]
     l.iane_gb_rl_run_host.restype = ctypes.c_int
+    l.iane_gb_rl_run_noalloc.argtypes = [_VIEW_P, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp]
+    l.iane_gb_rl_run_noalloc.restype = ctypes.c_int
     l.iane_gb_rl_destroy.argtypes = [vp]
     l.iane_gb_rl_destroy.restype = ctypes.c_int
     if l.iane_gb_abi_version() != abi.ABI_VERSION:

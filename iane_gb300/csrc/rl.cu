@@ -15,6 +15,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 struct iane_gb_rl_plan {
@@ -199,6 +200,142 @@ bool is_work_layout(const DevView& v, long long pitch)
 	if (v.ext[1] > 1 && v.stride[1] != pitch * 4) return false;
 	if (v.ext[2] > 1 && v.stride[2] != pitch * 4 * v.ext[1]) return false;
 	return true;
+}
+
+}  // namespace
+}  // namespace iane_gb
+
+// ------------------------------------------------------------------------------------
+// Allocation-free variant (iane_gb_rl_run_noalloc).
+//
+// Some callers cannot call cudaMalloc: code running while a CUDA graph is being captured
+// with a relaxed capture mode that forbids allocation, plugins loaded into a host that owns
+// the device allocator (a pooled allocator or a memory budget the plugin must not bypass),
+// and real-time loops that must not block in the driver's allocator. For them the variant
+// keeps every byte of RL's scratch -- ratio image, work estimate, sensitivity classes and
+// table, mean partials -- in the file-scope array below, sized for images of at most
+// kNoAllocMaxVoxels padded voxels. Every GPU that loads this library holds the array
+// (about 32.4 MiB) until the process exits.
+
+namespace iane_gb {
+namespace {
+
+constexpr long long kNoAllocMaxVoxels = 1LL << 22;  // round_up(nx, 4) * ny * nz
+constexpr int kNoAllocMaxAxisSum = 1 << 16;          // nx + ny + nz
+constexpr long long kNoAllocMaxTaps = 1LL << 15;     // PSF taps (also bounds the class table)
+constexpr int kNoAllocMaxExtent = 63;                // PSF extent per axis
+constexpr int kNoAllocMaxPartials = 4096;            // blocks of the mean reduction
+constexpr size_t kNoAllocImageBytes = static_cast<size_t>(kNoAllocMaxVoxels) * sizeof(float);
+constexpr size_t kNoAllocClsOffset = 2 * kNoAllocImageBytes;
+constexpr size_t kNoAllocTableOffset = kNoAllocClsOffset + kNoAllocMaxAxisSum * sizeof(int);
+constexpr size_t kNoAllocRangeOffset = kNoAllocTableOffset + kNoAllocMaxTaps * sizeof(float);
+constexpr size_t kNoAllocPartsOffset = kNoAllocRangeOffset + 256 * 3 * 2 * sizeof(int);
+constexpr size_t kNoAllocCounterOffset = kNoAllocPartsOffset + kNoAllocMaxPartials * sizeof(double);
+constexpr size_t kNoAllocBytes = kNoAllocCounterOffset + 256;
+
+}  // namespace
+}  // namespace iane_gb
+
+// The shared scratch of iane_gb_rl_run_noalloc. In host code this name is only a host-side
+// stand-in: the device address comes from cudaGetSymbolAddress (noalloc_scratch()).
+static __device__ __align__(256) unsigned char iane_gb_rl_noalloc_scratch[iane_gb::kNoAllocBytes];
+
+namespace iane_gb {
+namespace {
+
+// Device address of the array on the current device, looked up once per device with that
+// device current. Null on failure, with the error recorded.
+char* noalloc_scratch()
+{
+	static std::mutex lock;
+	static char* cached[64] = {};
+	int device = 0;
+	if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) {
+		set_error("rl_run_noalloc: no current CUDA device");
+		return nullptr;
+	}
+	std::lock_guard<std::mutex> guard(lock);
+	if (!cached[device]) {
+		void* p = nullptr;
+		const cudaError_t e = cudaGetSymbolAddress(&p, iane_gb_rl_noalloc_scratch);
+		if (e != cudaSuccess || !p) {
+			cuda_fail(e, "rl_run_noalloc: address of the static scratch");
+			return nullptr;
+		}
+		cached[device] = static_cast<char*>(p);
+	}
+	return cached[device];
+}
+
+// Number of sensitivity classes along one axis: the (first, last) tap ranges of
+// axis_classes() change monotonically with the coordinate, so classes are runs.
+int count_classes(int n, int k)
+{
+	const int c = k / 2;
+	int count = 0, last_lo = -1, last_hi = -1;
+	for (int p = 0; p < n; ++p) {
+		const int qlo = p + c - n + 1 > 0 ? p + c - n + 1 : 0;
+		const int qhi = p + c < k - 1 ? p + c : k - 1;
+		if (qlo != last_lo || qhi != last_hi) {
+			++count;
+			last_lo = qlo;
+			last_hi = qhi;
+		}
+	}
+	return count;
+}
+
+// Class index per coordinate (x at 0, y at nx, z at nx + ny) and each class's tap range,
+// numbered in order of appearance exactly as axis_classes() does on the host.
+__global__ void noalloc_classes_kernel(int nx, int ny, int nz, int kx, int ky, int kz, int* cls, int* ranges)
+{
+	const int axis = threadIdx.x;
+	if (axis >= 3) return;
+	const int n = axis == 0 ? nx : (axis == 1 ? ny : nz);
+	const int k = axis == 0 ? kx : (axis == 1 ? ky : kz);
+	int* out = cls + (axis == 0 ? 0 : (axis == 1 ? nx : nx + ny));
+	int* range = ranges + axis * 256 * 2;
+	const int c = k / 2;
+	int count = 0, last_lo = -1, last_hi = -1;
+	for (int p = 0; p < n; ++p) {
+		const int qlo = p + c - n + 1 > 0 ? p + c - n + 1 : 0;
+		const int qhi = p + c < k - 1 ? p + c : k - 1;
+		if (qlo != last_lo || qhi != last_hi) {
+			range[2 * count] = qlo;
+			range[2 * count + 1] = qhi;
+			++count;
+			last_lo = qlo;
+			last_hi = qhi;
+		}
+		out[p] = count - 1;
+	}
+}
+
+// Sensitivity of each class triple: the adjoint's zero-border response to an image of ones,
+// every tap in raster order with FP64 fma (1 inside the class's range, 0 outside), as the
+// reference's convolution_filter computes it; the adjoint tap q is PSF tap (k - 1 - q).
+__global__ void noalloc_table_kernel(DevView psf, const int* ranges, int cx, int cy, int cz, float* table)
+{
+	const int kx = psf.ext[0], ky = psf.ext[1], kz = psf.ext[2];
+	const int total = cx * cy * cz;
+	for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < total; id += gridDim.x * blockDim.x) {
+		const int ix = id % cx, iy = (id / cx) % cy, iz = id / (cx * cy);
+		const int* rx = ranges + 0 * 512 + 2 * ix;
+		const int* ry = ranges + 1 * 512 + 2 * iy;
+		const int* rz = ranges + 2 * 512 + 2 * iz;
+		double sum = 0.0;
+		for (int qz = 0; qz < kz; ++qz) {
+			for (int qy = 0; qy < ky; ++qy) {
+				for (int qx = 0; qx < kx; ++qx) {
+					const bool inside = qx >= rx[0] && qx <= rx[1] && qy >= ry[0] && qy <= ry[1] && qz >= rz[0] &&
+						qz <= rz[1];
+					const float k = *element_ptr<float>(psf, kx - 1 - qx, ky - 1 - qy, kz - 1 - qz);
+					sum = fma(inside ? 1.0 : 0.0, static_cast<double>(k), sum);
+				}
+			}
+		}
+		table[id] = static_cast<float>(sum);
+	}
 }
 
 }  // namespace
@@ -552,6 +689,167 @@ int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int ob
 	IANE_GB_CUDA(cudaMemcpy2DAsync(host_estimate, nx * 4, d_est, pitch * 4, nx * 4, static_cast<size_t>(ny) * nz,
 		cudaMemcpyDeviceToHost, st), "rl_run_host: download");
 	IANE_GB_CUDA(cudaStreamSynchronize(st), "rl_run_host: wait");
+	return IANE_GB_OK;
+}
+
+
+int iane_gb_rl_run_noalloc(const iane_gb_view* psf, const iane_gb_view* observed, const iane_gb_view* estimate,
+	int iterations, float epsilon, int init, void* stream)
+{
+	DevView k{}, obs{}, est{};
+	int status = normalise_view(psf, "rl_run_noalloc psf", &k);
+	if (status) return status;
+	status = normalise_view(observed, "rl_run_noalloc observed", &obs);
+	if (status) return status;
+	status = normalise_view(estimate, "rl_run_noalloc estimate", &est);
+	if (status) return status;
+	if (k.rank != obs.rank || est.rank != obs.rank) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run_noalloc: PSF, observed and estimate need the same rank");
+	}
+	for (int i = 0; i < 3; ++i) {
+		if (est.ext[i] != obs.ext[i]) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "Source and destination require matching nonnegative dimensions");
+		}
+		if (i < k.rank && (k.ext[i] <= 0 || k.ext[i] % 2 == 0)) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "Convolution requires positive odd kernel dimensions");
+		}
+	}
+	if (k.dtype != IANE_GB_F32) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_run_noalloc: the PSF must be f32");
+	}
+	if (obs.dtype != IANE_GB_F32 && obs.dtype != IANE_GB_U8) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_run_noalloc: observed image must be f32 or u8");
+	}
+	if (est.dtype != IANE_GB_F32 && est.dtype != IANE_GB_U8) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_run_noalloc: estimate must be f32 or u8");
+	}
+	if (iterations < 0 || !(epsilon > 0.0f) || !std::isfinite(epsilon)) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "Iterations and finite epsilon must be positive");
+	}
+	if (init < IANE_GB_RL_INIT_OBSERVED || init > IANE_GB_RL_INIT_GIVEN ||
+	    (init == IANE_GB_RL_INIT_GIVEN && est.dtype != IANE_GB_F32)) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_run_noalloc: unknown init mode or a given start without f32");
+	}
+	const int nx = obs.ext[0], ny = obs.ext[1], nz = obs.ext[2];
+	const long long pitch = (static_cast<long long>(nx) + 3) & ~3LL, plane = pitch * ny;
+	const long long taps = static_cast<long long>(k.ext[0]) * k.ext[1] * k.ext[2];
+	if (pitch * ny * nz > kNoAllocMaxVoxels || static_cast<long long>(nx) + ny + nz > kNoAllocMaxAxisSum) {
+		return fail(IANE_GB_LENGTH_ERROR, "rl_run_noalloc: image larger than the static scratch (at most 4194304 "
+			"voxels with rows padded to a multiple of 4, and nx + ny + nz <= 65536)");
+	}
+	if (k.ext[0] > 31 || k.ext[1] > kNoAllocMaxExtent || k.ext[2] > kNoAllocMaxExtent || taps > kNoAllocMaxTaps) {
+		return fail(IANE_GB_LENGTH_ERROR, "rl_run_noalloc: PSF larger than the static scratch allows (width <= 31, "
+			"height and depth <= 63, at most 32768 taps)");
+	}
+	if (element_count(obs) == 0) {
+		return IANE_GB_OK;
+	}
+	char* base = noalloc_scratch();
+	if (!base) return IANE_GB_CUDA_ERROR;
+	int* dstatus = device_status_ptr();
+	if (!dstatus) return IANE_GB_CUDA_ERROR;
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	float* ratio = reinterpret_cast<float*>(base);
+	float* work = reinterpret_cast<float*>(base + kNoAllocImageBytes);
+	int* cls = reinterpret_cast<int*>(base + kNoAllocClsOffset);
+	float* table = reinterpret_cast<float*>(base + kNoAllocTableOffset);
+	int* ranges = reinterpret_cast<int*>(base + kNoAllocRangeOffset);
+	double* parts = reinterpret_cast<double*>(base + kNoAllocPartsOffset);
+	unsigned int* counter = reinterpret_cast<unsigned int*>(base + kNoAllocCounterOffset);
+	float* start = reinterpret_cast<float*>(counter + 1);
+	const bool in_place = is_work_layout(est, pitch);
+	float* e_work = in_place ? reinterpret_cast<float*>(est.ptr) : work;
+	const long long n = static_cast<long long>(nx) * ny * nz;
+	const int ccount[3] = {count_classes(nx, k.ext[0]), count_classes(ny, k.ext[1]), count_classes(nz, k.ext[2])};
+
+	// The array keeps the previous call's contents: reset the completion counter.
+	IANE_GB_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned int), st), "rl_run_noalloc: clear counter");
+	noalloc_classes_kernel<<<1, 32, 0, st>>>(nx, ny, nz, k.ext[0], k.ext[1], k.ext[2], cls, ranges);
+	const int classes = ccount[0] * ccount[1] * ccount[2];
+	noalloc_table_kernel<<<(classes + 127) / 128, 128, 0, st>>>(k, ranges, ccount[0], ccount[1], ccount[2], table);
+	IANE_GB_CUDA(cudaGetLastError(), "rl_run_noalloc: launch table kernels");
+	if (init == IANE_GB_RL_INIT_GIVEN) {
+		if (!in_place) {
+			rl_copy_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est, 0);
+		}
+	} else {
+		if (init == IANE_GB_RL_INIT_MEAN) {
+			rl_mean_kernel<<<grid_for(n), 256, 0, st>>>(obs, parts, counter, start, epsilon);
+		}
+		rl_init_kernel<<<grid_for(n), 256, 0, st>>>(obs, e_work, pitch, plane, epsilon, init, start);
+	}
+	IANE_GB_CUDA(cudaGetLastError(), "rl_run_noalloc: launch init");
+
+	const long long big_tiles = static_cast<long long>((nx + 63) / 64) * ((ny + 63) / 64) * nz;
+	const bool small = big_tiles < 2LL * device_sm_count();
+	const int kx = k.ext[0];
+	const int wx = small ? 1 : 2;
+	const int wy = wx;
+	CUtensorMap map_est{}, map_ratio{};
+	status = encode_tensor_map_f32(&map_est, e_work, nx, ny, nz, pitch * 4, plane * 4, tile_pitch(kx, wx),
+		32 * wy + 2 * (k.ext[1] / 2));
+	if (status) return status;
+	status = encode_tensor_map_f32(&map_ratio, ratio, nx, ny, nz, pitch * 4, plane * 4, tile_pitch(kx, wx),
+		32 * wy + 2 * (k.ext[1] / 2));
+	if (status) return status;
+
+	TileArgs ta{};
+	ta.nx = nx;
+	ta.ny = ny;
+	ta.nz = nz;
+	ta.ky = k.ext[1];
+	ta.kz = k.ext[2];
+	ta.border = IANE_GB_BORDER_ZERO;
+	ta.status = dstatus;
+	TileArgs tb = ta;
+	// pass A reads the caller's PSF view as given; pass B reads it backwards along every
+	// axis, which is the adjoint, without a copy
+	ta.kernel = k.ptr;
+	tb.kernel = k.ptr + (k.ext[0] - 1) * k.stride[0] + (k.ext[1] - 1) * k.stride[1] + (k.ext[2] - 1) * k.stride[2];
+	for (int i = 0; i < 3; ++i) {
+		ta.k_stride[i] = k.stride[i];
+		tb.k_stride[i] = -k.stride[i];
+	}
+	EpiRatio ea{};
+	ea.ratio = ratio;
+	ea.pitch = pitch;
+	ea.plane = plane;
+	ea.obs = obs.ptr;
+	for (int i = 0; i < 3; ++i) ea.os[i] = obs.stride[i];
+	ea.obs_u8 = obs.dtype == IANE_GB_U8;
+	ea.eps = epsilon;
+	ea.nx = nx;
+	ea.ny = ny;
+	EpiUpdate eb{};
+	eb.est = e_work;
+	eb.pitch = pitch;
+	eb.plane = plane;
+	eb.eps = epsilon;
+	eb.nx = nx;
+	eb.ny = ny;
+	eb.nz = nz;
+	eb.cls = cls;
+	eb.sens = table;
+	eb.cx_count = ccount[0];
+	eb.cy_count = ccount[1];
+	for (int i = 0; i < 3; ++i) {
+		eb.ilo[i] = 1; // no interior shortcut: every voxel reads its class's table entry
+		eb.ihi[i] = 0;
+		eb.outs[i] = est.stride[i];
+	}
+	eb.out = est.ptr;
+	eb.out_u8 = est.dtype == IANE_GB_U8;
+	for (int it = 0; it < iterations; ++it) {
+		status = launch_rl_pass_a(kx, small, map_est, ta, ea, st);
+		if (status) return status;
+		eb.write_out = (!in_place && it == iterations - 1) ? 1 : 0;
+		status = launch_rl_pass_b(kx, small, map_ratio, tb, eb, st);
+		if (status) return status;
+	}
+	if (iterations == 0 && !in_place) {
+		rl_copy_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est, 1);
+		IANE_GB_CUDA(cudaGetLastError(), "rl_run_noalloc: launch copy-out");
+	}
 	return IANE_GB_OK;
 }
 

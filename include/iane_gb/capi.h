@@ -168,6 +168,30 @@ int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int ob
 /* Release a plan (after the stream has finished work that uses it). NULL is accepted. */
 int iane_gb_rl_destroy(iane_gb_rl_plan* plan);
 
+/*
+ * Allocation-free Richardson-Lucy. No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory: code recorded into a CUDA graph under
+ * a capture mode that forbids allocation, plugins inside a host application that owns the
+ * device allocator or enforces a memory budget, and latency-bound loops that cannot block
+ * in the allocator. It runs the same iteration as iane_gb_rl_prepare + iane_gb_rl_run, with
+ * the same kernels and results, but calls no cudaMalloc, cudaFree or other allocating
+ * routine: its scratch (ratio image, work estimate, edge-sensitivity table, reduction
+ * partials) is one static device array of about 32.4 MiB that every GPU loading this
+ * library keeps until the process exits. The caller passes the PSF (f32 device view, odd
+ * extents, the image rank, used as given), the observed image (f32 or u8) and the estimate
+ * (f32 or u8, as iane_gb_rl_run). Limits, rejected with IANE_GB_LENGTH_ERROR: at most
+ * 4194304 voxels counting rows padded to a multiple of 4, nx + ny + nz <= 65536, PSF width
+ * <= 31, height and depth <= 63, at most 32768 taps. No statistics are produced.
+ *
+ * The first call on a device looks up the array's device address with that device
+ * current; make that first call before any stream capture. All calls share the one array:
+ * calls whose GPU work overlaps (different streams, or different host threads, without
+ * ordering between them) race on it and corrupt each other's results.
+ */
+int iane_gb_rl_run_noalloc(const iane_gb_view* psf, const iane_gb_view* observed,
+	const iane_gb_view* estimate, int iterations, float epsilon, int init, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
