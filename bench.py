@@ -180,6 +180,53 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def measure_hbm_legs(dev, stream, reps=20):
+    """HBM-bound convolutions beside the main workload: the fused separable kernel on a
+    512^3 f32 volume (7-tap Gaussians, mirror border; 1 GiB in + out, larger than L2) and
+    the 2-D 512x512 7x7 Gaussian mirror case, direct and separable. Device time per launch
+    (CUDA events), algorithmic bytes = 8 per voxel (one read, one write)."""
+    import numpy as np
+    import torch
+
+    import iane_gb300
+    from iane_gb300 import synth
+
+    peaks, _ = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    g1 = torch.from_numpy(synth.gaussian_psf((7,), (1.5,))).to(dev)
+    g2 = torch.from_numpy(synth.gaussian_psf((7, 7), (1.5, 1.5))).to(dev)
+    out = {}
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / reps
+
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0)
+    vol = torch.rand((512, 512, 512), generator=gen, device=dev, dtype=torch.float32)
+    dst = torch.empty_like(vol)
+    ms = timed(lambda: iane_gb300.convolve_separable(vol, [g1, g1, g1], dst, "mirror", stream=stream))
+    gbs = 8.0 * vol.numel() / (ms / 1e3) / 1e9
+    out["separable_512^3_7tap_mirror"] = {"ms": ms, "gvoxel_s": vol.numel() / (ms / 1e3) / 1e9, "gbs": gbs,
+                                          "hbm_frac": gbs / hbm}
+    del vol, dst
+    img = torch.rand((512, 512), generator=gen, device=dev, dtype=torch.float32)
+    d2 = torch.empty_like(img)
+    ms = timed(lambda: iane_gb300.convolve(img, g2, d2, "mirror", stream=stream))
+    out["direct_512^2_7x7_mirror"] = {"ms": ms, "gvoxel_s": img.numel() / (ms / 1e3) / 1e9}
+    ms = timed(lambda: iane_gb300.convolve_separable(img, [g1, g1], d2, "mirror", stream=stream))
+    out["separable_512^2_7x7_mirror"] = {"ms": ms, "gvoxel_s": img.numel() / (ms / 1e3) / 1e9}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,6 +321,8 @@ def main():
         e2e_s = float(t.item())
     e2e_value = world * conv_voxels_per_step * e2e_steps / e2e_s / 1e9
 
+    hbm_legs = measure_hbm_legs(dev, stream)
+
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
     assert np.isfinite(est_np).all() and est_np.min() >= 0.0
@@ -328,6 +377,7 @@ def main():
             "gpu_launches": (2 + 2 * ITERATIONS) * args.steps,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+            "hbm_legs": hbm_legs,
         }
         print(json.dumps(line), flush=True)
     rl.close()
