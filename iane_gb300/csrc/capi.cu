@@ -312,6 +312,10 @@ int iane_gb_convolve_separable(const iane_gb_view* src, const iane_gb_view* cons
 	if (element_count(s) == 0) {
 		return IANE_GB_OK;
 	}
+	status = launch_conv_separable_fast(s, t, d, border, static_cast<cudaStream_t>(stream));
+	if (status != IANE_GB_UNSUPPORTED) {
+		return status;
+	}
 	return launch_conv_separable(s, t, d, border, static_cast<cudaStream_t>(stream));
 }
 

@@ -16,7 +16,12 @@ int launch_conv_generic(const DevView& src, const DevView& kernel, const DevView
 int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevView& dst, int border,
 	cudaStream_t stream);
 
-// Fused separable FP32 convolution (separable.cu).
+// Bandwidth-oriented fused separable FP32 convolution for radii <= 7 (separable_fast.cu);
+// IANE_GB_UNSUPPORTED without an error when it does not apply.
+int launch_conv_separable_fast(const DevView& src, const DevView* taps, const DevView& dst, int border,
+	cudaStream_t stream);
+
+// Fused separable FP32 convolution, any tap length (separable.cu).
 int launch_conv_separable(const DevView& src, const DevView* taps, const DevView& dst, int border,
 	cudaStream_t stream);
 

@@ -1,0 +1,345 @@
+// Bandwidth-oriented fused separable FP32 convolution (radius R <= 7 on every used axis).
+//
+// A block owns a 64 (x) x 16 (y) column of the volume and marches along z through a chunk
+// of planes. Per input plane:
+//   1. the (64 + 2 RA) x (16 + 2 R) halo tile lands in shared memory (double buffered): one
+//      TMA when the border is zero or the block is interior (zero fill = zero border), else
+//      4-byte cp.async with the border rule applied per element; RA = R rounded up to 4 so
+//      that the TMA's x start is 16-byte aligned;
+//   2. axis 0: each thread filters 4 consecutive x of one or two tile rows from a register
+//      window read with 128-bit shared loads, into a 64 x (16 + 2R) buffer;
+//   3. axis 1: each thread filters a 2 (x) x 2 (y) patch, the x pair as one float2 so that
+//      the multiply-adds are packed f32x2 FMAs (same tap, neighbouring columns);
+//   4. axis 2: the filtered patch enters a register window of 2R + 1 planes (the plane loop
+//      is unrolled by 2R + 1 so the window never moves) and, once full, produces the output
+//      plane R behind, written as float2 pairs.
+// Taps of every axis are zero-padded to 2R + 1, centred, so one radius serves all axes.
+// Rounding points are those of successive 1-D convolutions with an f32 intermediate.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace iane_gb {
+namespace {
+
+constexpr int kFX = 64;
+constexpr int kFY = 16;
+constexpr int kFThreads = 256;
+
+template<int R>
+struct SepGeom {
+	static constexpr int K = 2 * R + 1;
+	static constexpr int RA = (R + 3) & ~3;
+	static constexpr int D = RA - R;
+	static constexpr int AW = kFX + 2 * RA;            // tile width = TMA box width (floats)
+	static constexpr int AH = kFY + 2 * R;             // tile height
+	static constexpr int SEG = (D + 4 + 2 * R + 3) & ~3; // axis-0 window per thread
+	static constexpr int A_FLOATS = (AW * AH + 31) & ~31;
+	static constexpr int B_FLOATS = kFX * AH;
+};
+
+struct SepFastArgs {
+	const char* src;
+	long long s_stride[3];
+	char* dst;
+	long long d_stride[3];
+	int nx, ny, nz;
+	int border;
+	int zchunk;
+	int use_tma;      // source is TMA-addressable
+	int dst_pairs;    // destination rows take aligned float2 stores
+	int* status;
+	const char* tap_ptr[3];  // 1-D f32 device views of the taps (null: axis beyond the rank)
+	long long tap_stride[3];
+	int k[3];
+};
+
+template<int R, bool Z>
+__global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_constant__ CUtensorMap map,
+	const SepFastArgs a)
+{
+	using G = SepGeom<R>;
+	constexpr int K = G::K;
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	float* A = reinterpret_cast<float*>(smem_raw);           // 2 buffers
+	float* B = A + 2 * G::A_FLOATS;                           // axis-0 result
+	float2* tpair = reinterpret_cast<float2*>(B + G::B_FLOATS); // (t, t) pairs of axes 1 and 2
+	uint64_t* bars = reinterpret_cast<uint64_t*>(tpair + 2 * 16);
+
+	const int tid = threadIdx.x;
+	const int x0 = blockIdx.x * kFX, y0 = blockIdx.y * kFY;
+	const int zs = Z ? blockIdx.z * a.zchunk : 0;
+	const int ze = Z ? min(zs + a.zchunk, a.nz) : 1;
+	const int nplanes = Z ? (ze - zs) + 2 * R : 1;
+	const bool interior = x0 - G::RA >= 0 && x0 + kFX + G::RA <= a.nx && y0 - R >= 0 && y0 + kFY + R <= a.ny;
+	const bool tma = a.use_tma && (a.border == IANE_GB_BORDER_ZERO || interior);
+
+	// Taps centred and zero-padded to 2R + 1; an axis beyond the rank is the single tap 1.
+	auto tap = [&](int axis, int i) -> float {
+		if (!a.tap_ptr[axis]) {
+			return i == R ? 1.0f : 0.0f;
+		}
+		const int q = i - (R - a.k[axis] / 2);
+		return q >= 0 && q < a.k[axis] ? *reinterpret_cast<const float*>(a.tap_ptr[axis] + q * a.tap_stride[axis])
+			: 0.0f;
+	};
+	float tx[K];
+#pragma unroll
+	for (int i = 0; i < K; ++i) tx[i] = tap(0, i);
+	if (tid < 2 * K) {
+		const float t = tap(1 + tid / K, tid % K);
+		tpair[(tid / K) * 16 + tid % K] = make_float2(t, t);
+	}
+	if (tid == 0) {
+		mbar_init(&bars[0], 1);
+		mbar_init(&bars[1], 1);
+		fence_barrier_init();
+	}
+	__syncthreads();
+
+	// plane p of this block's sequence is input plane zs - R + p (Z) or 0
+	auto plane_of = [&](int p, int& zi) -> bool {
+		const int z = Z ? zs - R + p : 0;
+		return map_coord(z, a.nz, a.border, zi);
+	};
+	auto issue = [&](int p) {
+		float* dst = A + (p & 1) * G::A_FLOATS;
+		int zi = 0;
+		if (!plane_of(p, zi)) {
+			if (!tma) cp_async_commit(); // keep one cp.async group per plane
+			return; // zero-border plane outside the volume: never read
+		}
+		if (tma) {
+			if (tid == 0) {
+				mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(G::AW * G::AH * 4));
+				tma_load_3d(dst, &map, x0 - G::RA, y0 - R, zi, &bars[p & 1]);
+			}
+		} else {
+			const char* plane = a.src + zi * a.s_stride[2];
+			for (int i = tid; i < G::AW * G::AH; i += kFThreads) {
+				const int r = i / G::AW, c = i - r * G::AW;
+				int xi = 0, yi = 0;
+				const bool ok = map_coord(x0 - G::RA + c, a.nx, a.border, xi) && map_coord(y0 - R + r, a.ny, a.border, yi);
+				const char* s = ok ? plane + xi * a.s_stride[0] + yi * a.s_stride[1] : a.src;
+				cp_async4(dst + i, s, ok ? 4 : 0);
+			}
+			cp_async_commit();
+		}
+	};
+
+	// thread roles
+	const int xq = tid & 15, rg = tid >> 4;   // axis 0: 4 consecutive x of rows rg, rg + 16
+	const int xp = tid & 31, yq = tid >> 5;   // axes 1, 2: x pair 2xp, y rows 2yq, 2yq + 1
+	const int ox = x0 + 2 * xp, oy = y0 + 2 * yq;
+
+	float2 win[2][K]; // axis-2 window: [row][plane slot]
+#pragma unroll
+	for (int j = 0; j < 2; ++j)
+#pragma unroll
+		for (int s = 0; s < K; ++s) win[j][s] = make_float2(0.0f, 0.0f);
+
+	issue(0);
+	if (nplanes > 1) issue(1);
+	bool ok = true;
+	uint32_t waits0 = 0u, waits1 = 0u; // completed phases per tile buffer (absent planes load nothing)
+
+	// One plane: returns the axis-0/1 filtered 2x2 patch (zero for a zero-border plane).
+	auto filter_plane = [&](int p, float2& c0, float2& c1) {
+		int zi = 0;
+		const bool present = plane_of(p, zi);
+		if (present) {
+			if (tma) {
+				uint32_t& waits = (p & 1) ? waits1 : waits0;
+				if (ok && !mbar_wait_bounded(&bars[p & 1], waits & 1u)) {
+					ok = false;
+					report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
+				}
+				++waits;
+			} else {
+				if (p + 1 < nplanes) {
+					cp_async_wait<1>();
+				} else {
+					cp_async_wait<0>();
+				}
+			}
+		} else if (!tma) {
+			if (p + 1 < nplanes) {
+				cp_async_wait<1>();
+			} else {
+				cp_async_wait<0>();
+			}
+		}
+		__syncthreads(); // tile visible to all (cp.async path); B free
+		if (present) {
+			const float* tile = A + (p & 1) * G::A_FLOATS;
+#pragma unroll
+			for (int k = 0; k < 2; ++k) {
+				const int r = rg + 16 * k;
+				if (r < G::AH) {
+					float seg[G::SEG];
+					const float4* srow = reinterpret_cast<const float4*>(tile + r * G::AW + 4 * xq);
+#pragma unroll
+					for (int m = 0; m < G::SEG / 4; ++m) {
+						const float4 v = srow[m];
+						seg[4 * m] = v.x;
+						seg[4 * m + 1] = v.y;
+						seg[4 * m + 2] = v.z;
+						seg[4 * m + 3] = v.w;
+					}
+					float o[4];
+#pragma unroll
+					for (int i = 0; i < 4; ++i) {
+						float s = 0.0f;
+#pragma unroll
+						for (int q = 0; q < K; ++q) s = fmaf(tx[q], seg[G::D + i + 2 * R - q], s);
+						o[i] = s;
+					}
+					*reinterpret_cast<float4*>(B + r * kFX + 4 * xq) = make_float4(o[0], o[1], o[2], o[3]);
+				}
+			}
+		}
+		__syncthreads(); // B complete; tile buffer free
+		if (p + 2 < nplanes) issue(p + 2);
+		c0 = make_float2(0.0f, 0.0f);
+		c1 = make_float2(0.0f, 0.0f);
+		if (present) {
+			float2 col[2 + 2 * R];
+#pragma unroll
+			for (int m = 0; m < 2 + 2 * R; ++m) {
+				col[m] = *reinterpret_cast<const float2*>(B + (2 * yq + m) * kFX + 2 * xp);
+			}
+#pragma unroll
+			for (int q = 0; q < K; ++q) {
+				const float2 t = tpair[q];
+				c0 = __ffma2_rn(col[2 * R - q], t, c0);
+				c1 = __ffma2_rn(col[1 + 2 * R - q], t, c1);
+			}
+		}
+	};
+
+	auto store = [&](int zo, const float2& v0, const float2& v1) {
+#pragma unroll
+		for (int j = 0; j < 2; ++j) {
+			const int y = oy + j;
+			const float2 v = j == 0 ? v0 : v1;
+			if (y < a.ny) {
+				char* row = a.dst + y * a.d_stride[1] + zo * a.d_stride[2];
+				if (a.dst_pairs && ox + 1 < a.nx) {
+					*reinterpret_cast<float2*>(row + ox * 4LL) = v;
+				} else {
+					if (ox < a.nx) *reinterpret_cast<float*>(row + ox * a.d_stride[0]) = v.x;
+					if (ox + 1 < a.nx) *reinterpret_cast<float*>(row + (ox + 1) * a.d_stride[0]) = v.y;
+				}
+			}
+		}
+	};
+
+	if constexpr (!Z) {
+		float2 c0, c1;
+		filter_plane(0, c0, c1);
+		store(0, c0, c1);
+	} else {
+		// The window slot of plane p is p mod K; unrolling by K keeps every slot static.
+		for (int base = 0; base < nplanes; base += K) {
+#pragma unroll
+			for (int s = 0; s < K; ++s) {
+				const int p = base + s;
+				if (p < nplanes) {
+					filter_plane(p, win[0][s], win[1][s]);
+					if (p >= 2 * R) {
+						// output plane zs + p - 2R uses planes p - 2R .. p; tap q meets plane p - q
+						float2 o0 = make_float2(0.0f, 0.0f), o1 = make_float2(0.0f, 0.0f);
+#pragma unroll
+						for (int q = 0; q < K; ++q) {
+							const int slot = (s - q + K) % K;
+							const float2 t = tpair[16 + q];
+							o0 = __ffma2_rn(win[0][slot], t, o0);
+							o1 = __ffma2_rn(win[1][slot], t, o1);
+						}
+						store(zs + p - 2 * R, o0, o1);
+					}
+				}
+			}
+		}
+	}
+}
+
+template<int R>
+int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, int border, cudaStream_t stream)
+{
+	using G = SepGeom<R>;
+	SepFastArgs a{};
+	a.src = src.ptr;
+	a.dst = dst.ptr;
+	for (int i = 0; i < 3; ++i) {
+		a.s_stride[i] = src.stride[i];
+		a.d_stride[i] = dst.stride[i];
+	}
+	a.nx = src.ext[0];
+	a.ny = src.ext[1];
+	a.nz = src.ext[2];
+	a.border = border;
+	a.status = device_status_ptr();
+	if (!a.status) return IANE_GB_CUDA_ERROR;
+	for (int axis = 0; axis < 3; ++axis) {
+		a.tap_ptr[axis] = taps[axis].ptr;
+		a.tap_stride[axis] = taps[axis].stride[0];
+		a.k[axis] = taps[axis].ext[0];
+	}
+	const bool z3 = src.ext[2] > 1 || taps[2].ext[0] > 1;
+	a.use_tma = rows_aligned16(src) ? 1 : 0;
+	a.dst_pairs = (dst.stride[0] == 4 && reinterpret_cast<uintptr_t>(dst.ptr) % 8 == 0 &&
+		(dst.ext[1] <= 1 || dst.stride[1] % 8 == 0) && (dst.ext[2] <= 1 || dst.stride[2] % 8 == 0)) ? 1 : 0;
+	CUtensorMap map{};
+	if (a.use_tma) {
+		const long long row = src.ext[1] > 1 ? src.stride[1] : ((static_cast<long long>(src.ext[0]) * 4 + 15) & ~15LL);
+		const long long plane = src.ext[2] > 1 ? src.stride[2] : row * src.ext[1];
+		const int status = encode_tensor_map_f32(&map, src.ptr, src.ext[0], src.ext[1], src.ext[2], row, plane, G::AW,
+			G::AH);
+		if (status) return status;
+	}
+	const long long columns = static_cast<long long>((a.nx + kFX - 1) / kFX) * ((a.ny + kFY - 1) / kFY);
+	int chunk = a.nz;
+	const int sms = device_sm_count();
+	while (z3 && chunk > 4 * G::K && columns * ((a.nz + chunk - 1) / chunk) < 8LL * sms) {
+		chunk = (chunk + 1) / 2;
+	}
+	a.zchunk = chunk;
+	const size_t smem = (2 * G::A_FLOATS + G::B_FLOATS) * sizeof(float) + 2 * 16 * sizeof(float2) + 16;
+	const dim3 grid((a.nx + kFX - 1) / kFX, (a.ny + kFY - 1) / kFY, z3 ? (a.nz + chunk - 1) / chunk : 1);
+	if (z3) {
+		IANE_GB_CUDA(cudaFuncSetAttribute(separable_fast_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			static_cast<int>(smem)), "separable: set shared memory size");
+		separable_fast_kernel<R, true><<<grid, kFThreads, smem, stream>>>(map, a);
+	} else {
+		IANE_GB_CUDA(cudaFuncSetAttribute(separable_fast_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			static_cast<int>(smem)), "separable: set shared memory size");
+		separable_fast_kernel<R, false><<<grid, kFThreads, smem, stream>>>(map, a);
+	}
+	IANE_GB_CUDA(cudaGetLastError(), "separable: launch");
+	return IANE_GB_OK;
+}
+
+}  // namespace
+
+int launch_conv_separable_fast(const DevView& src, const DevView* taps, const DevView& dst, int border,
+	cudaStream_t stream)
+{
+	int r = 0;
+	for (int i = 0; i < 3; ++i) r = max(r, taps[i].ext[0] / 2);
+	if (src.stride[0] != 4 || r > 7 || src.ext[1] > 65535 * kFY || src.ext[2] > 65535 * 64) {
+		return IANE_GB_UNSUPPORTED;
+	}
+	switch (r) {
+	case 0:
+	case 1: return launch_radius<1>(src, taps, dst, border, stream);
+	case 2: return launch_radius<2>(src, taps, dst, border, stream);
+	case 3: return launch_radius<3>(src, taps, dst, border, stream);
+	case 4: return launch_radius<4>(src, taps, dst, border, stream);
+	case 5: return launch_radius<5>(src, taps, dst, border, stream);
+	case 6: return launch_radius<6>(src, taps, dst, border, stream);
+	case 7: return launch_radius<7>(src, taps, dst, border, stream);
+	default: return IANE_GB_UNSUPPORTED;
+	}
+}
+
+}  // namespace iane_gb

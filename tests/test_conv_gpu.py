@@ -179,11 +179,13 @@ def test_rl_volume_convolution_slabs(cuda):
 
 @pytest.mark.parametrize("border", ["clamp", "zero", "mirror"])
 @pytest.mark.parametrize("shape,taps", [((40,), (7,)), ((33, 70), (7, 7)), ((512, 512), (7, 7)), ((9, 30, 75), (5, 3, 7)),
-                                       ((20, 20, 20), (9, 9, 9)), ((3, 5, 4), (7, 9, 11))])
+                                       ((20, 20, 20), (9, 9, 9)), ((3, 5, 4), (7, 9, 11)), ((70, 90), (21, 3)),
+                                       ((37, 41, 130), (15, 15, 15)), ((1, 1, 1), (3, 3, 3)), ((17, 1, 200), (3, 5, 1)),
+                                       ((64, 64, 64), (3, 3, 3))])
 def test_separable_parity(cuda, shape, taps, border):
     rng = np.random.default_rng(len(shape) * 100 + taps[0])
     src = rng.random(shape, dtype=np.float32)
-    tap_list = [gaussian((n,), (1.5,)) for n in taps]
+    tap_list = [gaussian((n,), (max(0.5, n / 5),)) for n in taps]
     ref = np.zeros_like(src)
     oracle.convolve_separable(src, tap_list, ref, border)
     d = empty_like_np(shape, np.float32)
@@ -191,6 +193,23 @@ def test_separable_parity(cuda, shape, taps, border):
     out = to_host(d)
     # each 1-D pass accumulates in FP32; positive data and taps
     assert float(np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1e-30))) <= FP32_TOL
+
+
+def test_separable_strided_views(cuda):
+    t = torch()
+    rng = np.random.default_rng(8)
+    big = rng.random((30, 70, 90), dtype=np.float32)
+    src_np = np.ascontiguousarray(big[3:27, 5:65:2, 1:88])
+    g = to_gpu(big)[3:27, 5:65:2, 1:88]
+    taps = [gaussian((n,), (1.2,)) for n in (5, 7, 3)]
+    for border in ("clamp", "zero", "mirror"):
+        ref = np.zeros_like(src_np)
+        oracle.convolve_separable(src_np, taps, ref, border)
+        dst_big = t.zeros((24, 30, 200), device="cuda")
+        dst = dst_big[:, :, 3:3 + 2 * src_np.shape[2]:2]
+        iane_gb300.convolve_separable(g, [to_gpu(x) for x in taps], dst, border)
+        out = to_host(dst)
+        assert float(np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1e-30))) <= FP32_TOL
 
 
 def test_separable_equals_direct_outer_product(cuda):
