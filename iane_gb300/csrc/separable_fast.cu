@@ -286,7 +286,10 @@ int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, i
 		a.k[axis] = taps[axis].ext[0];
 	}
 	const bool z3 = src.ext[2] > 1 || taps[2].ext[0] > 1;
-	a.use_tma = rows_aligned16(src) ? 1 : 0;
+	// TMA wants positive, 16-byte multiple pitches that do not make rows or planes overlap.
+	a.use_tma = (rows_aligned16(src) && (src.ext[1] <= 1 || src.stride[1] >= 4LL * src.ext[0]) &&
+		(src.ext[2] <= 1 || (src.stride[2] > 0 && src.stride[2] >= (src.ext[1] > 1 ? src.stride[1] : 4LL * src.ext[0]) *
+			src.ext[1]))) ? 1 : 0;
 	a.dst_pairs = (dst.stride[0] == 4 && reinterpret_cast<uintptr_t>(dst.ptr) % 8 == 0 &&
 		(dst.ext[1] <= 1 || dst.stride[1] % 8 == 0) && (dst.ext[2] <= 1 || dst.stride[2] % 8 == 0)) ? 1 : 0;
 	CUtensorMap map{};
