@@ -2,8 +2,9 @@
 //
 // A block owns a 64 (x) x 16 (y) column of the volume and marches along z through a chunk
 // of planes. Per input plane:
-//   1. the (64 + 2 RA) x (16 + 2 R) halo tile lands in shared memory (double buffered): one
-//      TMA when the border is zero or the block is interior (zero fill = zero border), else
+//   1. the (64 + 2 RA) x (16 + 2 R) halo tile lands in shared memory, three planes ahead of
+//      the one being filtered (four buffers): one TMA when the border is zero or the block is
+//      interior (zero fill = zero border; planes outside the volume load as zeros), else
 //      4-byte cp.async with the border rule applied per element; RA = R rounded up to 4 so
 //      that the TMA's x start is 16-byte aligned;
 //   2. axis 0: each thread filters 4 consecutive x of one or two tile rows from a register
@@ -24,6 +25,7 @@ namespace {
 constexpr int kFX = 64;
 constexpr int kFY = 16;
 constexpr int kFThreads = 256;
+constexpr int kNBuf = 4; // tile buffers: three planes load while one is filtered
 
 template<int R>
 struct SepGeom {
@@ -60,8 +62,8 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	using G = SepGeom<R>;
 	constexpr int K = G::K;
 	extern __shared__ __align__(128) unsigned char smem_raw[];
-	float* A = reinterpret_cast<float*>(smem_raw);           // 2 buffers
-	float* B = A + 2 * G::A_FLOATS;                           // axis-0 result
+	float* A = reinterpret_cast<float*>(smem_raw);           // kNBuf tile buffers
+	float* B = A + kNBuf * G::A_FLOATS;                       // axis-0 result
 	float2* tpair = reinterpret_cast<float2*>(B + G::B_FLOATS); // (t, t) pairs of axes 1 and 2
 	uint64_t* bars = reinterpret_cast<uint64_t*>(tpair + 2 * 16);
 
@@ -90,8 +92,7 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 		tpair[(tid / K) * 16 + tid % K] = make_float2(t, t);
 	}
 	if (tid == 0) {
-		mbar_init(&bars[0], 1);
-		mbar_init(&bars[1], 1);
+		for (int b = 0; b < kNBuf; ++b) mbar_init(&bars[b], 1);
 		fence_barrier_init();
 	}
 	__syncthreads();
@@ -102,18 +103,19 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 		return map_coord(z, a.nz, a.border, zi);
 	};
 	auto issue = [&](int p) {
-		float* dst = A + (p & 1) * G::A_FLOATS;
+		float* dst = A + (p % kNBuf) * G::A_FLOATS;
 		int zi = 0;
-		if (!plane_of(p, zi)) {
-			if (!tma) cp_async_commit(); // keep one cp.async group per plane
-			return; // zero-border plane outside the volume: never read
-		}
+		const bool present = plane_of(p, zi);
 		if (tma) {
+			// every plane gets one TMA (an out-of-volume plane reads as zeros), so the k-th
+			// completion of buffer b belongs to plane b + k * kNBuf
 			if (tid == 0) {
-				mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(G::AW * G::AH * 4));
-				tma_load_3d(dst, &map, x0 - G::RA, y0 - R, zi, &bars[p & 1]);
+				mbar_arrive_expect_tx(&bars[p % kNBuf], static_cast<uint32_t>(G::AW * G::AH * 4));
+				tma_load_3d(dst, &map, x0 - G::RA, y0 - R, present ? zi : (Z ? zs - R + p : 0), &bars[p % kNBuf]);
 			}
-		} else {
+			return;
+		}
+		if (present) {
 			const char* plane = a.src + zi * a.s_stride[2];
 			for (int i = tid; i < G::AW * G::AH; i += kFThreads) {
 				const int r = i / G::AW, c = i - r * G::AW;
@@ -122,8 +124,8 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 				const char* s = ok ? plane + xi * a.s_stride[0] + yi * a.s_stride[1] : a.src;
 				cp_async4(dst + i, s, ok ? 4 : 0);
 			}
-			cp_async_commit();
 		}
+		cp_async_commit(); // one group per plane, empty for a zero-border plane outside
 	};
 
 	// thread roles
@@ -137,32 +139,27 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 #pragma unroll
 		for (int s = 0; s < K; ++s) win[j][s] = make_float2(0.0f, 0.0f);
 
-	issue(0);
-	if (nplanes > 1) issue(1);
+	for (int p = 0; p < kNBuf - 1 && p < nplanes; ++p) issue(p);
 	bool ok = true;
-	uint32_t waits0 = 0u, waits1 = 0u; // completed phases per tile buffer (absent planes load nothing)
 
 	// One plane: returns the axis-0/1 filtered 2x2 patch (zero for a zero-border plane).
 	auto filter_plane = [&](int p, float2& c0, float2& c1) {
 		int zi = 0;
-		const bool present = plane_of(p, zi);
-		if (present) {
-			if (tma) {
-				uint32_t& waits = (p & 1) ? waits1 : waits0;
-				if (ok && !mbar_wait_bounded(&bars[p & 1], waits & 1u)) {
-					ok = false;
-					report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
-				}
-				++waits;
-			} else {
-				if (p + 1 < nplanes) {
-					cp_async_wait<1>();
-				} else {
-					cp_async_wait<0>();
-				}
+		const bool present = tma || plane_of(p, zi);
+		if (p + kNBuf - 1 < nplanes) issue(p + kNBuf - 1); // its buffer held plane p - 1
+		if (tma) {
+			if (ok && !mbar_wait_bounded(&bars[p % kNBuf], (p / kNBuf) & 1)) {
+				ok = false;
+				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
-		} else if (!tma) {
-			if (p + 1 < nplanes) {
+		} else {
+			// groups committed after plane p's: planes p+1 .. min(p+3, last)
+			const int newer = min(kNBuf - 1, nplanes - 1 - p);
+			if (newer >= 3) {
+				cp_async_wait<3>();
+			} else if (newer == 2) {
+				cp_async_wait<2>();
+			} else if (newer == 1) {
 				cp_async_wait<1>();
 			} else {
 				cp_async_wait<0>();
@@ -170,7 +167,7 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 		}
 		__syncthreads(); // tile visible to all (cp.async path); B free
 		if (present) {
-			const float* tile = A + (p & 1) * G::A_FLOATS;
+			const float* tile = A + (p % kNBuf) * G::A_FLOATS;
 #pragma unroll
 			for (int k = 0; k < 2; ++k) {
 				const int r = rg + 16 * k;
@@ -197,8 +194,7 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 				}
 			}
 		}
-		__syncthreads(); // B complete; tile buffer free
-		if (p + 2 < nplanes) issue(p + 2);
+		__syncthreads(); // B complete; this tile buffer is free for plane p + kNBuf
 		c0 = make_float2(0.0f, 0.0f);
 		c1 = make_float2(0.0f, 0.0f);
 		if (present) {
@@ -307,7 +303,8 @@ int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, i
 		chunk = (chunk + 1) / 2;
 	}
 	a.zchunk = chunk;
-	const size_t smem = (2 * G::A_FLOATS + G::B_FLOATS) * sizeof(float) + 2 * 16 * sizeof(float2) + 16;
+	const size_t smem = (kNBuf * G::A_FLOATS + G::B_FLOATS) * sizeof(float) + 2 * 16 * sizeof(float2) +
+		kNBuf * sizeof(uint64_t);
 	const dim3 grid((a.nx + kFX - 1) / kFX, (a.ny + kFY - 1) / kFY, z3 ? (a.nz + chunk - 1) / chunk : 1);
 	if (z3) {
 		IANE_GB_CUDA(cudaFuncSetAttribute(separable_fast_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
