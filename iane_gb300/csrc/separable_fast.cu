@@ -3,17 +3,18 @@
 // A block owns a 64 (x) x 16 (y) column of the volume and marches along z through a chunk
 // of planes. Per input plane:
 //   1. the (64 + 2 RA) x (16 + 2 R) halo tile lands in shared memory, three planes ahead of
-//      the one being filtered (four buffers): one TMA when the border is zero or the block is
-//      interior (zero fill = zero border; planes outside the volume load as zeros), else
-//      4-byte cp.async with the border rule applied per element; RA = R rounded up to 4 so
-//      that the TMA's x start is 16-byte aligned;
+//      the one being filtered (four buffers), by one TMA (zero fill outside the image = the
+//      zero border; planes outside the volume load as zeros). For clamp and mirror borders
+//      the block then rewrites only its out-of-image halo cells from their mapped in-image
+//      cells. Views TMA cannot address use 4-byte cp.async with the border rule applied per
+//      element. RA = R rounded up to 4 so that the TMA's x start is 16-byte aligned;
 //   2. axis 0: each thread filters 4 consecutive x of one or two tile rows from a register
 //      window read with 128-bit shared loads, into a 64 x (16 + 2R) buffer;
 //   3. axis 1: each thread filters a 2 (x) x 2 (y) patch, the x pair as one float2 so that
 //      the multiply-adds are packed f32x2 FMAs (same tap, neighbouring columns);
-//   4. axis 2: the filtered patch enters a register window of 2R + 1 planes (the plane loop
-//      is unrolled by 2R + 1 so the window never moves) and, once full, produces the output
-//      plane R behind, written as float2 pairs.
+//   4. axis 2: the filtered patch enters a register window of 2R + 1 planes (shifted by one
+//      slot per plane) and, once full, produces the output plane R behind, written as float2
+//      pairs.
 // Taps of every axis are zero-padded to 2R + 1, centred, so one radius serves all axes.
 // Rounding points are those of successive 1-D convolutions with an f32 intermediate.
 #include "common.cuh"
@@ -73,7 +74,8 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	const int ze = Z ? min(zs + a.zchunk, a.nz) : 1;
 	const int nplanes = Z ? (ze - zs) + 2 * R : 1;
 	const bool interior = x0 - G::RA >= 0 && x0 + kFX + G::RA <= a.nx && y0 - R >= 0 && y0 + kFY + R <= a.ny;
-	const bool tma = a.use_tma && (a.border == IANE_GB_BORDER_ZERO || interior);
+	const bool tma = a.use_tma;
+	const bool fixup = tma && !interior && a.border != IANE_GB_BORDER_ZERO;
 
 	// Taps centred and zero-padded to 2R + 1; an axis beyond the rank is the single tap 1.
 	auto tap = [&](int axis, int i) -> float {
@@ -110,6 +112,10 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 			// every plane gets one TMA (an out-of-volume plane reads as zeros), so the k-th
 			// completion of buffer b belongs to plane b + k * kNBuf
 			if (tid == 0) {
+				if (fixup) {
+					// order this buffer's earlier generic-proxy writes (the fix-up) before the TMA
+					asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+				}
 				mbar_arrive_expect_tx(&bars[p % kNBuf], static_cast<uint32_t>(G::AW * G::AH * 4));
 				tma_load_3d(dst, &map, x0 - G::RA, y0 - R, present ? zi : (Z ? zs - R + p : 0), &bars[p % kNBuf]);
 			}
@@ -165,7 +171,31 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 				cp_async_wait<0>();
 			}
 		}
-		__syncthreads(); // tile visible to all (cp.async path); B free
+		if (fixup) {
+			// clamp / mirror: replace the zero-filled out-of-image halo cells by the cells the
+			// border rule maps them to (inside this tile, else read from the image)
+			float* tile = A + (p % kNBuf) * G::A_FLOATS;
+			int zi2 = 0;
+			plane_of(p, zi2);
+			const int gx0 = x0 - G::RA, gy0 = y0 - R;
+			const int c_lo = max(0, -gx0), c_hi = min(G::AW, a.nx - gx0); // in-image columns [c_lo, c_hi)
+			for (int r = tid >> 5; r < G::AH; r += kFThreads / 32) {
+				const int gy = gy0 + r;
+				const bool row_in = gy >= 0 && gy < a.ny;
+				for (int c = tid & 31; c < G::AW; c += 32) {
+					if (row_in && c >= c_lo && c < c_hi) continue;
+					int mx = 0, my = 0;
+					map_coord(gx0 + c, a.nx, a.border, mx);
+					map_coord(gy, a.ny, a.border, my);
+					const int lc = mx - gx0, lr = my - gy0;
+					const bool in_image_cell = lc >= c_lo && lc < c_hi && lr >= 0 && lr < G::AH && my >= 0;
+					tile[r * G::AW + c] = in_image_cell ? tile[lr * G::AW + lc]
+						: *reinterpret_cast<const float*>(a.src + mx * a.s_stride[0] + my * a.s_stride[1] +
+							zi2 * a.s_stride[2]);
+				}
+			}
+		}
+		__syncthreads(); // tile visible to all; B free
 		if (present) {
 			const float* tile = A + (p % kNBuf) * G::A_FLOATS;
 #pragma unroll
@@ -234,26 +264,26 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 		filter_plane(0, c0, c1);
 		store(0, c0, c1);
 	} else {
-		// The window slot of plane p is p mod K; unrolling by K keeps every slot static.
-		for (int base = 0; base < nplanes; base += K) {
+		for (int p = 0; p < nplanes; ++p) {
+			float2 n0, n1;
+			filter_plane(p, n0, n1);
 #pragma unroll
-			for (int s = 0; s < K; ++s) {
-				const int p = base + s;
-				if (p < nplanes) {
-					filter_plane(p, win[0][s], win[1][s]);
-					if (p >= 2 * R) {
-						// output plane zs + p - 2R uses planes p - 2R .. p; tap q meets plane p - q
-						float2 o0 = make_float2(0.0f, 0.0f), o1 = make_float2(0.0f, 0.0f);
+			for (int q = 0; q < K - 1; ++q) {
+				win[0][q] = win[0][q + 1];
+				win[1][q] = win[1][q + 1];
+			}
+			win[0][K - 1] = n0;
+			win[1][K - 1] = n1;
+			if (p >= 2 * R) {
+				// output plane zs + p - 2R uses planes p - 2R .. p; tap q meets plane p - q
+				float2 o0 = make_float2(0.0f, 0.0f), o1 = make_float2(0.0f, 0.0f);
 #pragma unroll
-						for (int q = 0; q < K; ++q) {
-							const int slot = (s - q + K) % K;
-							const float2 t = tpair[16 + q];
-							o0 = __ffma2_rn(win[0][slot], t, o0);
-							o1 = __ffma2_rn(win[1][slot], t, o1);
-						}
-						store(zs + p - 2 * R, o0, o1);
-					}
+				for (int q = 0; q < K; ++q) {
+					const float2 t = tpair[16 + q];
+					o0 = __ffma2_rn(win[0][K - 1 - q], t, o0);
+					o1 = __ffma2_rn(win[1][K - 1 - q], t, o1);
 				}
+				store(zs + p - 2 * R, o0, o1);
 			}
 		}
 	}
