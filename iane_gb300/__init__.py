@@ -92,13 +92,20 @@ class RichardsonLucy:
     INIT_MEAN = abi.RL_INIT_MEAN
     INIT_GIVEN = abi.RL_INIT_GIVEN
 
-    def __init__(self, psf, shape, stream=None):
+    def __init__(self, psf, shape, stream=None, precision: str = "f32"):
+        """``precision="bf16"`` selects the tensor-core path: BF16 images and PSF in the
+        convolutions (tcgen05 implicit GEMM, FP32 accumulation), FP32 everything else."""
         self.shape = tuple(int(s) for s in shape)
+        self.precision = precision
+        if precision not in ("f32", "bf16"):
+            raise ValueError(f"unknown precision {precision!r}")
         rank = len(self.shape)
         ext = (ctypes.c_int32 * 3)(*([self.shape[rank - 1 - i] for i in range(rank)] + [1] * (3 - rank)))
         handle = ctypes.c_void_p()
         v = _device_view(psf)
-        check(lib().iane_gb_rl_prepare(ctypes.byref(v), rank, ext, _stream_handle(stream), ctypes.byref(handle)))
+        flags = abi.RL_BF16_TENSOR if precision == "bf16" else 0
+        check(lib().iane_gb_rl_prepare_ex(ctypes.byref(v), rank, ext, flags, _stream_handle(stream),
+                                          ctypes.byref(handle)))
         self._plan = handle
         self.scratch_bytes = int(lib().iane_gb_rl_scratch_bytes(handle))
 

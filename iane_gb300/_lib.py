@@ -61,6 +61,8 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_convolve_separable.restype = ctypes.c_int
     l.iane_gb_rl_prepare.argtypes = [_VIEW_P, ctypes.c_int, i32p, vp, ctypes.POINTER(vp)]
     l.iane_gb_rl_prepare.restype = ctypes.c_int
+    l.iane_gb_rl_prepare_ex.argtypes = [_VIEW_P, ctypes.c_int, i32p, ctypes.c_uint, vp, ctypes.POINTER(vp)]
+    l.iane_gb_rl_prepare_ex.restype = ctypes.c_int
     l.iane_gb_rl_scratch_bytes.argtypes = [cvp]
     l.iane_gb_rl_scratch_bytes.restype = ctypes.c_size_t
     l.iane_gb_rl_run.argtypes = [vp, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp,

@@ -113,6 +113,12 @@ bool rows_aligned16(const DevView& v)
 int encode_tensor_map_f32(CUtensorMap* map, const void* base, int nx, int ny, int nz, long long row_pitch,
 	long long plane_pitch, int bx, int by)
 {
+	return encode_tensor_map(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, base, nx, ny, nz, row_pitch, plane_pitch, bx, by);
+}
+
+int encode_tensor_map(CUtensorMap* map, int data_type, const void* base, int nx, int ny, int nz, long long row_pitch,
+	long long plane_pitch, int bx, int by)
+{
 	using encode_fn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
 		const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
 		CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -134,7 +140,7 @@ int encode_tensor_map_f32(CUtensorMap* map, const void* base, int nx, int ny, in
 	const cuuint64_t strides[2] = {static_cast<cuuint64_t>(row_pitch), static_cast<cuuint64_t>(plane_pitch)};
 	const cuuint32_t box[3] = {static_cast<cuuint32_t>(bx), static_cast<cuuint32_t>(by), 1};
 	const cuuint32_t estride[3] = {1, 1, 1};
-	const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box,
+	const CUresult r = encode(map, static_cast<CUtensorMapDataType>(data_type), 3, const_cast<void*>(base), dims, strides, box,
 		estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
 		CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	if (r != CUDA_SUCCESS) {

@@ -224,6 +224,9 @@ template<int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("
 // row_pitch (dim 1) and plane_pitch (dim 2), box (bx, by, 1), zero fill out of bounds.
 int encode_tensor_map_f32(CUtensorMap* map, const void* base, int nx, int ny, int nz,
 	long long row_pitch, long long plane_pitch, int bx, int by);
+// The same for any CUtensorMapDataType (e.g. CU_TENSOR_MAP_DATA_TYPE_BFLOAT16).
+int encode_tensor_map(CUtensorMap* map, int data_type, const void* base, int nx, int ny, int nz,
+	long long row_pitch, long long plane_pitch, int bx, int by);
 
 int device_sm_count();
 

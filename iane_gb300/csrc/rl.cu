@@ -12,6 +12,7 @@
 //   misc   : block-completion counter and the flat-start value
 #include "kernels.h"
 #include "rl.cuh"
+#include "rl_tc.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -36,6 +37,12 @@ struct iane_gb_rl_plan {
 	size_t scratch_bytes;
 	bool small_tiles;
 	long long pass_blocks;
+	// BF16 tensor-core precision path (IANE_GB_RL_BF16_TENSOR)
+	bool bf16;
+	__nv_bfloat16* d_tmat_psf; // banded T matrices per kernel row, psf and adjoint
+	__nv_bfloat16* d_tmat_adj;
+	long long pitch16;         // bf16 elements per work-image row (multiple of 8)
+	size_t image16_bytes;
 };
 
 namespace iane_gb {
@@ -206,6 +213,135 @@ bool is_work_layout(const DevView& v, long long pitch)
 }  // namespace iane_gb
 
 // ------------------------------------------------------------------------------------
+// BF16 tensor-core precision path (plans prepared with IANE_GB_RL_BF16_TENSOR).
+
+namespace iane_gb {
+namespace {
+
+__global__ void rl_to_bf16_kernel(const float* e, long long pitch, long long plane, __nv_bfloat16* d, long long pitch16,
+	long long plane16, int nx, int ny, int nz)
+{
+	const long long n = static_cast<long long>(nx) * ny * nz;
+	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
+		const int x = static_cast<int>(i % nx);
+		const int y = static_cast<int>((i / nx) % ny);
+		const int z = static_cast<int>(i / (static_cast<long long>(nx) * ny));
+		d[z * plane16 + y * pitch16 + x] = __float2bfloat16_rn(e[z * plane + y * pitch + x]);
+	}
+}
+
+int rl_run_bf16(iane_gb_rl_plan* plan, const DevView& obs, const DevView& est, int iterations, float epsilon, int init,
+	char* base, double* stats, cudaStream_t st)
+{
+	const int nx = plan->ext[0], ny = plan->ext[1], nz = plan->ext[2];
+	const long long pitch = plan->pitch, plane = pitch * ny;
+	const long long p16 = plan->pitch16, plane16 = p16 * ny;
+	float* work = reinterpret_cast<float*>(base);
+	__nv_bfloat16* est16 = reinterpret_cast<__nv_bfloat16*>(base + plan->image_bytes);
+	__nv_bfloat16* ratio16 = reinterpret_cast<__nv_bfloat16*>(base + plan->image_bytes + plan->image16_bytes);
+	double* parts = reinterpret_cast<double*>(base + plan->image_bytes + 2 * plan->image16_bytes);
+	unsigned int* counter = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(parts) + plan->parts_bytes);
+	float* start = reinterpret_cast<float*>(counter + 1);
+	const bool in_place = is_work_layout(est, pitch);
+	float* e_work = in_place ? reinterpret_cast<float*>(est.ptr) : work;
+	const long long n = static_cast<long long>(nx) * ny * nz;
+
+	IANE_GB_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned int), st), "rl_run: clear counter");
+	if (init == IANE_GB_RL_INIT_GIVEN) {
+		if (!in_place) {
+			rl_copy_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est, 0);
+		}
+	} else {
+		if (init == IANE_GB_RL_INIT_MEAN) {
+			rl_mean_kernel<<<grid_for(n), 256, 0, st>>>(obs, parts, counter, start, epsilon);
+		}
+		rl_init_kernel<<<grid_for(n), 256, 0, st>>>(obs, e_work, pitch, plane, epsilon, init, start);
+	}
+	rl_to_bf16_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est16, p16, plane16, nx, ny, nz);
+	IANE_GB_CUDA(cudaGetLastError(), "rl_run: launch init");
+
+	int* dstatus = device_status_ptr();
+	if (!dstatus) return IANE_GB_CUDA_ERROR;
+	const int ky = plan->k[1];
+	CUtensorMap map_est{}, map_ratio{};
+	int status = encode_tensor_map(&map_est, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, est16, nx, ny, nz, p16 * 2, plane16 * 2,
+		8, tc_rows(ky));
+	if (status) return status;
+	status = encode_tensor_map(&map_ratio, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ratio16, nx, ny, nz, p16 * 2, plane16 * 2,
+		8, tc_rows(ky));
+	if (status) return status;
+
+	TcArgs ta{};
+	ta.nx = nx;
+	ta.ny = ny;
+	ta.nz = nz;
+	ta.ky = ky;
+	ta.kz = plan->k[2];
+	ta.status = dstatus;
+	// Generous margins: the whole TMEM and 200 KB of shared memory per CTA.
+	ta.smem_bytes = static_cast<int>(tc_smem_bytes(ky) > 200 * 1024 ? tc_smem_bytes(ky) : 200 * 1024);
+	ta.tmem_cols = 512;
+	TcArgs tb = ta;
+	ta.tmat = plan->d_tmat_psf;
+	tb.tmat = plan->d_tmat_adj;
+
+	EpiRatioTc ea{};
+	ea.ratio = ratio16;
+	ea.pitch = p16;
+	ea.plane = plane16;
+	ea.obs = obs.ptr;
+	for (int i = 0; i < 3; ++i) ea.os[i] = obs.stride[i];
+	ea.obs_u8 = obs.dtype == IANE_GB_U8;
+	ea.eps = epsilon;
+	ea.nx = nx;
+	ea.ny = ny;
+
+	EpiUpdateTc eb{};
+	eb.est = e_work;
+	eb.pitch = pitch;
+	eb.plane = plane;
+	eb.est16 = est16;
+	eb.pitch16 = p16;
+	eb.plane16 = plane16;
+	eb.eps = epsilon;
+	eb.nx = nx;
+	eb.ny = ny;
+	eb.nz = nz;
+	eb.cls = plan->d_cls;
+	eb.sens = plan->d_sens;
+	eb.cx_count = plan->ccount[0];
+	eb.cy_count = plan->ccount[1];
+	for (int i = 0; i < 3; ++i) {
+		eb.ilo[i] = plan->ilo[i];
+		eb.ihi[i] = plan->ihi[i];
+		eb.outs[i] = est.stride[i];
+	}
+	eb.s_interior = plan->s_interior;
+	eb.partials = parts;
+	eb.counter = counter;
+	eb.out = est.ptr;
+	eb.out_u8 = est.dtype == IANE_GB_U8;
+	for (int it = 0; it < iterations; ++it) {
+		status = launch_tc_pass_a(map_est, ta, ea, st);
+		if (status) return status;
+		eb.want_stats = stats != nullptr;
+		eb.stats = stats ? stats + 2 * it : nullptr;
+		eb.write_out = (!in_place && it == iterations - 1) ? 1 : 0;
+		status = launch_tc_pass_b(map_ratio, tb, eb, st);
+		if (status) return status;
+	}
+	if (iterations == 0 && !in_place) {
+		rl_copy_kernel<<<grid_for(n), 256, 0, st>>>(e_work, pitch, plane, est, 1);
+		IANE_GB_CUDA(cudaGetLastError(), "rl_run: launch copy-out");
+	}
+	return IANE_GB_OK;
+}
+
+}  // namespace
+}  // namespace iane_gb
+
+// ------------------------------------------------------------------------------------
 // Allocation-free variant (iane_gb_rl_run_noalloc).
 //
 // Some callers cannot call cudaMalloc: code running while a CUDA graph is being captured
@@ -345,8 +481,13 @@ using namespace iane_gb;
 
 extern "C" {
 
-int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent, void* stream, iane_gb_rl_plan** out)
+static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* extent, unsigned flags, void* stream,
+	iane_gb_rl_plan** out)
 {
+	const bool bf16 = (flags & IANE_GB_RL_BF16_TENSOR) != 0;
+	if (flags & ~IANE_GB_RL_BF16_TENSOR) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: unknown flags");
+	}
 	if (!out || !extent) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: null argument");
 	}
@@ -373,6 +514,9 @@ int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
 	if (k.ext[0] > 31 || k.ext[1] > 63) {
 		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: PSF wider than 31 along axis 0 or 63 along axis 1");
 	}
+	if (bf16 && k.ext[0] > 17) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: the BF16 tensor-core path takes PSFs up to 17 wide");
+	}
 	const long long taps = static_cast<long long>(k.ext[0]) * k.ext[1] * k.ext[2];
 	if (taps * ((k.ext[0] + 3) & ~3) / k.ext[0] * 4 > 96 * 1024) {
 		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: PSF too large for shared memory");
@@ -380,6 +524,7 @@ int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	auto* plan = new iane_gb_rl_plan{};
 	plan->rank = rank;
+	plan->bf16 = bf16;
 	for (int i = 0; i < 3; ++i) {
 		plan->ext[i] = ext[i];
 		plan->k[i] = k.ext[i];
@@ -403,6 +548,13 @@ int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
 		if (!std::isfinite(h_psf[i])) {
 			return cleanup(fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: PSF coefficients must be finite"));
 		}
+		if (bf16) {
+			// the precision path convolves with the bf16-rounded PSF; everything derived
+			// from it (adjoint, sensitivity) uses those same values
+			h_psf[i] = __bfloat162float(__float2bfloat16_rn(h_psf[i]));
+		}
+	}
+	for (long long i = 0; i < taps; ++i) {
 		h_adj[i] = h_psf[taps - 1 - i]; // reverse_copy of the packed PSF (main.cu:106-107)
 	}
 	// Sensitivity = zero-border convolution of an all-ones image with the adjoint
@@ -444,6 +596,31 @@ int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
 	    cudaMalloc(&plan->d_sens, table.size() * sizeof(float)) != cudaSuccess) {
 		return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: allocate sensitivity tables"));
 	}
+	if (bf16) {
+		// T_{b,qz}[k][n] = kernel[qz][b][n + rx + 8 - k], stored [qz][b][k / 8][n][k % 8]
+		const int kx = k.ext[0], ky = k.ext[1], kz = k.ext[2], rx = kx / 2;
+		const size_t per = static_cast<size_t>(kTcTmatBytes / 2);
+		std::vector<__nv_bfloat16> tp(static_cast<size_t>(kz) * ky * per), ta(tp.size());
+		for (int qz = 0; qz < kz; ++qz)
+			for (int b = 0; b < ky; ++b)
+				for (int kk = 0; kk < 32; ++kk)
+					for (int n = 0; n < 16; ++n) {
+						const int tap = n + rx + kTcXA - kk;
+						const size_t at = (static_cast<size_t>(qz) * ky + b) * per + (kk / 8) * 128 + n * 8 + kk % 8;
+						const size_t src = (static_cast<size_t>(qz) * ky + b) * kx + tap;
+						tp[at] = __float2bfloat16_rn(tap >= 0 && tap < kx ? h_psf[src] : 0.0f);
+						ta[at] = __float2bfloat16_rn(tap >= 0 && tap < kx ? h_adj[src] : 0.0f);
+					}
+		if (cudaMalloc(&plan->d_tmat_psf, tp.size() * sizeof(__nv_bfloat16)) != cudaSuccess ||
+		    cudaMalloc(&plan->d_tmat_adj, ta.size() * sizeof(__nv_bfloat16)) != cudaSuccess ||
+		    cudaMemcpyAsync(plan->d_tmat_psf, tp.data(), tp.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, st) !=
+		        cudaSuccess ||
+		    cudaMemcpyAsync(plan->d_tmat_adj, ta.data(), ta.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, st) !=
+		        cudaSuccess ||
+		    cudaStreamSynchronize(st) != cudaSuccess) {
+			return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: upload tensor-core matrices"));
+		}
+	}
 	if (cudaMemcpyAsync(plan->d_adj, h_adj.data(), taps * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
 	    (!all_cls.empty() && cudaMemcpyAsync(plan->d_cls, all_cls.data(), all_cls.size() * sizeof(int),
 	                         cudaMemcpyHostToDevice, st) != cudaSuccess) ||
@@ -463,8 +640,28 @@ int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
 	plan->parts_bytes = round_up(static_cast<size_t>(
 		(plan->pass_blocks * 3 > mean_blocks ? plan->pass_blocks * 3 : mean_blocks) * sizeof(double)), kAlign);
 	plan->scratch_bytes = 2 * plan->image_bytes + plan->parts_bytes + 2 * kAlign;
+	if (bf16) {
+		// scratch: f32 work estimate, bf16 estimate shadow, bf16 ratio, partials, counter
+		plan->pitch16 = (static_cast<long long>(ext[0]) + 7) & ~7LL;
+		plan->image16_bytes = round_up(static_cast<size_t>(plan->pitch16) * ext[1] * ext[2] * 2, kAlign);
+		plan->pass_blocks = static_cast<long long>((ext[0] + kTcN - 1) / kTcN) * ((ext[1] + kTcM - 1) / kTcM) * ext[2];
+		plan->parts_bytes = round_up(static_cast<size_t>(
+			(plan->pass_blocks * 3 > mean_blocks ? plan->pass_blocks * 3 : mean_blocks) * sizeof(double)), kAlign);
+		plan->scratch_bytes = plan->image_bytes + 2 * plan->image16_bytes + plan->parts_bytes + 2 * kAlign;
+	}
 	*out = plan;
 	return IANE_GB_OK;
+}
+
+int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent, void* stream, iane_gb_rl_plan** out)
+{
+	return rl_prepare_impl(psf, rank, extent, 0u, stream, out);
+}
+
+int iane_gb_rl_prepare_ex(const iane_gb_view* psf, int rank, const int32_t* extent, unsigned flags, void* stream,
+	iane_gb_rl_plan** out)
+{
+	return rl_prepare_impl(psf, rank, extent, flags, stream, out);
 }
 
 size_t iane_gb_rl_scratch_bytes(const iane_gb_rl_plan* plan)
@@ -481,6 +678,8 @@ int iane_gb_rl_destroy(iane_gb_rl_plan* plan)
 	cudaFree(plan->d_adj);
 	cudaFree(plan->d_cls);
 	cudaFree(plan->d_sens);
+	cudaFree(plan->d_tmat_psf);
+	cudaFree(plan->d_tmat_adj);
 	delete plan;
 	return IANE_GB_OK;
 }
@@ -527,8 +726,11 @@ int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const ia
 	}
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	char* base = reinterpret_cast<char*>(round_up(reinterpret_cast<uintptr_t>(scratch), kAlign));
-	if (base + 2 * plan->image_bytes + plan->parts_bytes + 8 > static_cast<char*>(scratch) + scratch_bytes) {
+	if (base + (plan->scratch_bytes - 2 * kAlign) + 8 > static_cast<char*>(scratch) + scratch_bytes) {
 		return fail(IANE_GB_LENGTH_ERROR, "Prepared operation exceeded its scratch reservation");
+	}
+	if (plan->bf16) {
+		return rl_run_bf16(plan, obs, est, iterations, epsilon, init, base, stats, static_cast<cudaStream_t>(stream));
 	}
 	float* ratio = reinterpret_cast<float*>(base);
 	float* work = reinterpret_cast<float*>(base + plan->image_bytes);

@@ -141,6 +141,16 @@ typedef struct iane_gb_rl_plan iane_gb_rl_plan;
 int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
 	void* stream, iane_gb_rl_plan** plan);
 
+/* Precision path: images and PSF in BF16 for the convolutions, which run as implicit GEMMs
+ * on the tcgen05 tensor cores with FP32 accumulation; the ratio, the division guard, the
+ * update and the statistics stay FP32 (the estimate keeps an FP32 master copy). PSFs up to
+ * 17 wide. No counterpart in the reference, which convolves in FP64. */
+#define IANE_GB_RL_BF16_TENSOR 1u
+
+/* iane_gb_rl_prepare with flags (0 or IANE_GB_RL_BF16_TENSOR). */
+int iane_gb_rl_prepare_ex(const iane_gb_view* psf, int rank, const int32_t* extent,
+	unsigned flags, void* stream, iane_gb_rl_plan** plan);
+
 /* Scratch bytes iane_gb_rl_run needs (ratio image, statistics), 256-byte aligned. */
 size_t iane_gb_rl_scratch_bytes(const iane_gb_rl_plan* plan);
 

@@ -1,0 +1,87 @@
+"""The BF16 tensor-core Richardson-Lucy path (tcgen05 implicit GEMM, FP32 accumulation).
+
+Two checks: one iteration against an FP64 host emulation of exactly what the path computes
+(bf16 operands, FP32 ratio/update), which pins the GEMM formulation; and full runs against
+the FP64-accumulating CPU oracle, reporting max-abs and relative-L2 error."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import iane_gb300
+import oracle
+from gpu_helpers import empty_like_np, gaussian, rel_l2, to_gpu, to_host, torch
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(a: np.ndarray) -> np.ndarray:
+    """Round float32 values to bfloat16 (nearest, ties to even), returned as float32."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def conv64(src, kernel):
+    out = np.zeros(src.shape, np.float64)
+    oracle.convolve(src.astype(np.float64), kernel.astype(np.float64), out, "zero")
+    return out
+
+
+@pytest.mark.parametrize("shape,pshape", [((8, 72, 130), (9, 9, 9)), ((3, 140, 70), (3, 5, 7)), ((1, 40, 64), (1, 9, 17))])
+def test_one_iteration_matches_bf16_emulation(cuda, shape, pshape):
+    rng = np.random.default_rng(sum(shape) + sum(pshape))
+    psf = bf16(gaussian(pshape, [max(0.7, n / 4) for n in pshape]))
+    obs = (rng.random(shape) * 500 + 5).astype(np.float32)
+    est0 = bf16((rng.random(shape) * 400 + 20).astype(np.float32))
+    eps = np.float32(1e-6)
+    pred = conv64(est0, psf).astype(np.float32)
+    ratio = bf16(obs / np.maximum(pred, eps))
+    adj = np.ascontiguousarray(psf[::-1, ::-1, ::-1])
+    corr = conv64(ratio, adj).astype(np.float32)
+    sens = oracle.sensitivity(adj, shape)
+    factor = np.where(sens > 0, corr / np.maximum(sens, eps), np.float32(0)).astype(np.float32)
+    expected = est0 * factor
+
+    rl = iane_gb300.RichardsonLucy(to_gpu(psf), shape, precision="bf16")
+    est = to_gpu(est0.copy())
+    rl.run(to_gpu(obs), est, 1, 1e-6, init=rl.INIT_GIVEN)
+    got = to_host(est)
+    iane_gb300.device_status()
+    rl.close()
+    # FP32 accumulation in the tensor core against FP64 here; a ratio voxel may round to
+    # the neighbouring bf16 value, which moves its neighbours by ~0.4% of one PSF weight
+    assert rel_l2(got, expected) <= 1e-3, rel_l2(got, expected)
+    assert float(np.max(np.abs(got - expected) / np.abs(expected))) <= 1e-2
+
+
+def test_bf16_rl_error_against_fp64_oracle(cuda):
+    rng = np.random.default_rng(3)
+    shape = (24, 96, 100)
+    grids = np.meshgrid(*[np.arange(n, dtype=np.float32) for n in shape], indexing="ij")
+    truth = np.full(shape, 10.0, np.float32)
+    for _ in range(25):
+        c = [rng.uniform(0, n) for n in shape]
+        r = [rng.uniform(2, 8) for _ in shape]
+        truth[sum(((g - ci) / ri) ** 2 for g, ci, ri in zip(grids, c, r)) <= 1] += rng.uniform(50, 1000)
+    psf = gaussian((9, 9, 9), (2.5, 2.5, 2.5))
+    obs = rng.poisson(np.maximum(conv64(truth, psf), 0)).astype(np.float32)
+    ref = oracle.rl(obs, psf, 20, 1e-6, init=1)
+    f32 = iane_gb300.RichardsonLucy(to_gpu(psf), shape)
+    e32 = empty_like_np(shape, np.float32)
+    f32.run(to_gpu(obs), e32, 20, 1e-6, init=1)
+    b16 = iane_gb300.RichardsonLucy(to_gpu(psf), shape, precision="bf16")
+    e16 = empty_like_np(shape, np.float32)
+    stats = torch().zeros(40, dtype=torch().float64, device="cuda")
+    b16.run(to_gpu(obs), e16, 20, 1e-6, init=1, stats=stats)
+    got32, got16 = to_host(e32), to_host(e16)
+    err16 = rel_l2(got16, ref)
+    err32 = rel_l2(got32, ref)
+    print(f"bf16 path: rel-L2 {err16:.3e}, max-abs {np.max(np.abs(got16 - ref)):.3e}; "
+          f"f32 path: rel-L2 {err32:.3e}")
+    assert err32 <= 1e-5
+    assert err16 <= 2e-2
+    s = to_host(stats).reshape(-1, 2)
+    assert np.all(np.isfinite(s)) and s[-1, 1] < s[0, 1]
+    f32.close()
+    b16.close()
