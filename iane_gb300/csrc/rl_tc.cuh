@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(128, 1) tc_conv_kernel(const __grid_constant__
 	if (!mbar_wait_bounded(done, 0)) {
 		report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 	}
+	__syncwarp(); // tcgen05.ld is warp-collective
 	tc::fence_after_sync();
 	float v[kTcN];
 #pragma unroll
