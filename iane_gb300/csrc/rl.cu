@@ -279,9 +279,8 @@ int rl_run_bf16(iane_gb_rl_plan* plan, const DevView& obs, const DevView& est, i
 	ta.ky = ky;
 	ta.kz = plan->k[2];
 	ta.status = dstatus;
-	// Generous margins: the whole TMEM and 200 KB of shared memory per CTA.
-	ta.smem_bytes = static_cast<int>(tc_smem_bytes(ky) > 200 * 1024 ? tc_smem_bytes(ky) : 200 * 1024);
-	ta.tmem_cols = 512;
+	ta.smem_bytes = static_cast<int>(tc_smem_bytes(ky));
+	ta.tmem_cols = kTcTmemCols;
 	TcArgs tb = ta;
 	ta.tmat = plan->d_tmat_psf;
 	tb.tmat = plan->d_tmat_adj;

@@ -55,7 +55,7 @@ struct TcArgs {
 };
 
 template<class Epi>
-__global__ void __launch_bounds__(128, 1) tc_conv_kernel(const __grid_constant__ CUtensorMap map, const TcArgs a,
+__global__ void __launch_bounds__(128, 2) tc_conv_kernel(const __grid_constant__ CUtensorMap map, const TcArgs a,
 	const Epi epi_in)
 {
 	extern __shared__ __align__(128) unsigned char smem_raw[];

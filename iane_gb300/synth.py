@@ -63,3 +63,12 @@ def rl_volume_workload(seed=0):
     psf = gaussian_psf((15, 15, 7), (2.0, 2.0, 1.0))
     observed = poisson(blur_zero_border(truth, psf), seed=seed + 1)
     return observed, psf, truth
+
+
+def rl_volume_workload_bf16(seed=0):
+    """The 3-D RL precision-path input: the same 256x256x64 ellipsoid phantom blurred by the
+    normalised isotropic 9x9x9 Gaussian PSF with sigma 2.5, with Poisson noise."""
+    truth = ellipsoid_phantom((256, 256, 64), 200, seed=seed)
+    psf = gaussian_psf((9, 9, 9), (2.5, 2.5, 2.5))
+    observed = poisson(blur_zero_border(truth, psf), seed=seed + 1)
+    return observed, psf, truth
