@@ -158,23 +158,25 @@ __global__ void __launch_bounds__(128, 2) tc_conv_kernel(const __grid_constant__
 		for (int i = 0; i < 16; ++i) v[16 * j + i] = part[i];
 	}
 	tc::fence_before_sync();
+	// Transpose through shared memory (the stages are idle now): thread = row above, warp =
+	// row below, so that every global access of the epilogue is a coalesced row segment.
+	float* E = reinterpret_cast<float*>(smem_raw);
+	constexpr int EP = kTcN + 1; // pitch: thread t writes row t without bank conflicts
+#pragma unroll
+	for (int i = 0; i < kTcN; ++i) E[tid * EP + i] = v[i];
 	__syncthreads();
 	if (warp == 0) {
 		tc::tmem_dealloc(tmem, static_cast<uint32_t>(a.tmem_cols));
 	}
 	Epi epi = epi_in;
-	epi.row(x0, y0 + 32 * warp + lane, z, v);
+	for (int r = warp; r < kTcM; r += 4) {
+		epi.row_pair(x0 + lane, y0 + r, z, E[r * EP + lane], E[r * EP + lane + 32]);
+	}
 	epi.finish();
 }
 
 // ---------------------------------------------------------------------------------------
 // epilogues
-
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
-{
-	const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
-	return *reinterpret_cast<const uint32_t*>(&p);
-}
 
 // pass A: ratio = observed / max(pred, eps), stored as bf16 (the next convolution's input)
 struct EpiRatioTc {
@@ -186,34 +188,20 @@ struct EpiRatioTc {
 	float eps;
 	int nx, ny;
 
-	__device__ __forceinline__ void row(int x0, int y, int z, const float (&v)[kTcN]) const
+	// one warp, one row: this lane's columns x and x + 32
+	__device__ __forceinline__ void row_pair(int x, int y, int z, float p0, float p1) const
 	{
 		if (y >= ny) return;
-		__nv_bfloat16* out = ratio + z * plane + y * pitch + x0;
+		__nv_bfloat16* out = ratio + z * plane + y * pitch;
 		const char* orow = obs + y * os[1] + z * os[2];
 #pragma unroll
-		for (int g = 0; g < kTcN / 8; ++g) {
-			float r[8];
-#pragma unroll
-			for (int i = 0; i < 8; ++i) {
-				const int x = x0 + 8 * g + i;
-				float o = 0.0f;
-				if (x < nx) {
-					const char* p = orow + x * os[0];
-					o = obs_u8 ? static_cast<float>(*reinterpret_cast<const uint8_t*>(p)) : *reinterpret_cast<const float*>(p);
-				}
-				const float pr = v[8 * g + i];
-				r[i] = o / (pr > eps ? pr : eps);
-			}
-			if (x0 + 8 * g + 8 <= nx) {
-				uint4 pk = make_uint4(pack_bf16x2(r[0], r[1]), pack_bf16x2(r[2], r[3]), pack_bf16x2(r[4], r[5]),
-					pack_bf16x2(r[6], r[7]));
-				*reinterpret_cast<uint4*>(out + 8 * g) = pk;
-			} else {
-#pragma unroll
-				for (int i = 0; i < 8; ++i) {
-					if (x0 + 8 * g + i < nx) out[8 * g + i] = __float2bfloat16_rn(r[i]);
-				}
+		for (int h = 0; h < 2; ++h) {
+			const int xx = x + 32 * h;
+			if (xx < nx) {
+				const char* q = orow + xx * os[0];
+				const float o = obs_u8 ? static_cast<float>(*reinterpret_cast<const uint8_t*>(q)) : *reinterpret_cast<const float*>(q);
+				const float pr = h ? p1 : p0;
+				out[xx] = __float2bfloat16_rn(o / (pr > eps ? pr : eps));
 			}
 		}
 	}
@@ -244,61 +232,37 @@ struct EpiUpdateTc {
 	int out_u8;
 	float f_s, f_c, c_s, c_c, n_s, n_c;
 
-	__device__ __forceinline__ void row(int x0, int y, int z, const float (&v)[kTcN])
+	__device__ __forceinline__ void row_pair(int x, int y, int z, float c0, float c1)
 	{
 		if (y >= ny) return;
 		const bool rows_in = y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
 		const int cyz = cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
-		float* e = est + z * plane + y * pitch + x0;
-		__nv_bfloat16* e16 = est16 + z * plane16 + y * pitch16 + x0;
+		float* e = est + z * plane + y * pitch;
+		__nv_bfloat16* e16 = est16 + z * plane16 + y * pitch16;
 #pragma unroll
-		for (int g = 0; g < kTcN / 8; ++g) {
-			const bool full = x0 + 8 * g + 8 <= nx;
-			float old[8], upd[8];
-			if (full) {
-				const float4 p0 = reinterpret_cast<const float4*>(e + 8 * g)[0];
-				const float4 p1 = reinterpret_cast<const float4*>(e + 8 * g)[1];
-				old[0] = p0.x; old[1] = p0.y; old[2] = p0.z; old[3] = p0.w;
-				old[4] = p1.x; old[5] = p1.y; old[6] = p1.z; old[7] = p1.w;
-			} else {
-#pragma unroll
-				for (int i = 0; i < 8; ++i) old[i] = x0 + 8 * g + i < nx ? e[8 * g + i] : 0.0f;
+		for (int h = 0; h < 2; ++h) {
+			const int xx = x + 32 * h;
+			if (xx >= nx) continue;
+			float s = s_interior;
+			if (!(rows_in && xx >= ilo[0] && xx <= ihi[0])) s = sens[cls[xx] + cyz];
+			const float cv = h ? c1 : c0;
+			const float factor = s > 0.0f ? cv / (s > eps ? s : eps) : 0.0f;
+			const float old = e[xx];
+			const float upd = old * factor;
+			e[xx] = upd;
+			e16[xx] = __float2bfloat16_rn(upd);
+			if (want_stats) {
+				kahan_add(f_s, f_c, upd);
+				const float d = upd - old;
+				kahan_add(c_s, c_c, d * d);
+				kahan_add(n_s, n_c, old * old);
 			}
-#pragma unroll
-			for (int i = 0; i < 8; ++i) {
-				const int x = x0 + 8 * g + i;
-				float s = s_interior;
-				if (!(rows_in && x >= ilo[0] && x <= ihi[0]) && x < nx) s = sens[cls[x] + cyz];
-				const float factor = s > 0.0f ? v[8 * g + i] / (s > eps ? s : eps) : 0.0f;
-				upd[i] = old[i] * factor;
-			}
-			if (full) {
-				reinterpret_cast<float4*>(e + 8 * g)[0] = make_float4(upd[0], upd[1], upd[2], upd[3]);
-				reinterpret_cast<float4*>(e + 8 * g)[1] = make_float4(upd[4], upd[5], upd[6], upd[7]);
-				*reinterpret_cast<uint4*>(e16 + 8 * g) = make_uint4(pack_bf16x2(upd[0], upd[1]),
-					pack_bf16x2(upd[2], upd[3]), pack_bf16x2(upd[4], upd[5]), pack_bf16x2(upd[6], upd[7]));
-			}
-#pragma unroll
-			for (int i = 0; i < 8; ++i) {
-				const int x = x0 + 8 * g + i;
-				if (x >= nx) continue;
-				if (!full) {
-					e[8 * g + i] = upd[i];
-					e16[8 * g + i] = __float2bfloat16_rn(upd[i]);
-				}
-				if (want_stats) {
-					kahan_add(f_s, f_c, upd[i]);
-					const float d = upd[i] - old[i];
-					kahan_add(c_s, c_c, d * d);
-					kahan_add(n_s, n_c, old[i] * old[i]);
-				}
-				if (write_out) {
-					char* p = out + x * outs[0] + y * outs[1] + z * outs[2];
-					if (out_u8) {
-						*reinterpret_cast<uint8_t*>(p) = to_gray8(upd[i]);
-					} else {
-						*reinterpret_cast<float*>(p) = upd[i];
-					}
+			if (write_out) {
+				char* q = out + xx * outs[0] + y * outs[1] + z * outs[2];
+				if (out_u8) {
+					*reinterpret_cast<uint8_t*>(q) = to_gray8(upd);
+				} else {
+					*reinterpret_cast<float*>(q) = upd;
 				}
 			}
 		}
