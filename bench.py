@@ -269,6 +269,52 @@ def measure_bf16_leg(dev, stream, reps=5):
     return out
 
 
+def measure_batch_leg(dev, stream, reps=3, iterations=30):
+    """Batched uneven 2-D RL: 256 images, sides log-uniform in [64, 1024], own Gaussian PSF
+    each (odd size 3-31, sigma 0.5-5), Poisson noise, 30 iterations, one CUDA-graph replay
+    per run of persistent work-queue passes, autotuned tile shapes."""
+    import numpy as np
+    import torch
+
+    import iane_gb300
+    from iane_gb300 import synth
+
+    truths, psfs = synth.batch_workload(count=256, seed=0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0)
+    g_psfs = [torch.from_numpy(p).to(dev) for p in psfs]
+    obs = []
+    for t, p in zip(truths, g_psfs):
+        src = torch.from_numpy(t).to(dev)
+        blurred = torch.empty_like(src)
+        iane_gb300.convolve(src, p, blurred, "zero", stream=stream)
+        obs.append(torch.poisson(blurred.clamp_min(0), generator=gen))
+    outs = [torch.empty_like(o) for o in obs]
+    t0 = time.perf_counter()
+    batch = iane_gb300.RichardsonLucyBatch(g_psfs, [o.shape for o in obs], autotune=True)
+    prepare_s = time.perf_counter() - t0
+    scratch = torch.empty(batch.scratch_bytes, dtype=torch.uint8, device=dev)
+    batch.run(obs, outs, iterations, EPSILON, init=1, scratch=scratch, stream=stream)  # captures the graph
+    torch.cuda.synchronize(dev)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        batch.run(obs, outs, iterations, EPSILON, init=1, scratch=scratch, stream=stream)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / reps
+    pixels = sum(o.numel() for o in obs)
+    macs = sum(o.numel() * p.numel() for o, p in zip(obs, psfs)) * 2 * iterations
+    widths = batch.tile_widths()
+    batch.close()
+    assert all(bool(torch.isfinite(o).all()) for o in outs)
+    return {"images": len(obs), "pixels": pixels, "iterations": iterations, "ms_per_run": ms,
+            "gvoxel_s": 2 * iterations * pixels / (ms / 1e3) / 1e9, "tflops_useful": 2 * macs / (ms / 1e3) / 1e12,
+            "tiles_64": int(sum(1 for w in widths if w == 64)), "tiles_32": int(sum(1 for w in widths if w == 32)),
+            "prepare_s": prepare_s}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -365,6 +411,7 @@ def main():
 
     hbm_legs = measure_hbm_legs(dev, stream)
     bf16_leg = measure_bf16_leg(dev, stream)
+    batch_leg = measure_batch_leg(dev, stream)
 
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
@@ -422,6 +469,7 @@ def main():
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
             "hbm_legs": hbm_legs,
             "bf16_tensor_leg": bf16_leg,
+            "batch_leg": batch_leg,
         }
         print(json.dumps(line), flush=True)
     rl.close()

@@ -22,7 +22,7 @@ from . import abi
 from ._lib import IaneError, IaneInvalidArgument, IaneLengthError, check, lib
 
 __all__ = [
-    "abi", "convolve", "convolve_separable", "RichardsonLucy", "device_status", "IaneError",
+    "abi", "convolve", "convolve_separable", "RichardsonLucy", "RichardsonLucyBatch", "device_status", "IaneError",
     "IaneInvalidArgument", "IaneLengthError",
 ]
 
@@ -154,6 +154,57 @@ class RichardsonLucy:
         if self._plan is not None:
             lib().iane_gb_rl_destroy(self._plan)
             self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RichardsonLucyBatch:
+    """Richardson-Lucy over many 2-D images of uneven size, each with its own PSF.
+
+    One persistent launch per pass and tile shape over a device work queue; the schedule of
+    a run is captured into a CUDA graph and replayed while the tensors and parameters stay
+    the same. ``autotune=True`` times 32x32 against 64x64 tiles per (shape, PSF size) and
+    caches the choice (file named by ``IANE_GB_TUNE_CACHE``)."""
+
+    def __init__(self, psfs, shapes, autotune: bool = False, stream=None):
+        self.shapes = [tuple(int(v) for v in s) for s in shapes]
+        if len(psfs) != len(self.shapes) or not psfs:
+            raise ValueError("one PSF per image shape, at least one image")
+        self._psf_views = (abi.View * len(psfs))(*[_device_view(p) for p in psfs])
+        ext = (ctypes.c_int32 * (2 * len(psfs)))(*[v for (ny, nx) in self.shapes for v in (nx, ny)])
+        handle = ctypes.c_void_p()
+        flags = abi.BATCH_AUTOTUNE if autotune else 0
+        check(lib().iane_gb_rl_batch_prepare(self._psf_views, len(psfs), ext, flags, _stream_handle(stream),
+                                             ctypes.byref(handle)))
+        self._batch = handle
+        self.scratch_bytes = int(lib().iane_gb_rl_batch_scratch_bytes(handle))
+
+    def tile_widths(self):
+        out = (ctypes.c_int32 * len(self.shapes))()
+        check(lib().iane_gb_rl_batch_tiles(self._batch, out))
+        return list(out)
+
+    def run(self, observed, estimates, iterations: int, epsilon: float = 1e-6, init: int = abi.RL_INIT_OBSERVED,
+            scratch=None, stream=None):
+        import torch
+
+        if scratch is None:
+            scratch = torch.empty(self.scratch_bytes, dtype=torch.uint8, device=observed[0].device)
+        self._keep = (observed, estimates, scratch)
+        o = (abi.View * len(observed))(*[_device_view(t) for t in observed])
+        e = (abi.View * len(estimates))(*[_device_view(t) for t in estimates])
+        check(lib().iane_gb_rl_batch_run(self._batch, o, e, int(iterations), ctypes.c_float(epsilon), int(init),
+                                         scratch.data_ptr(), scratch.numel(), _stream_handle(stream)))
+        return estimates
+
+    def close(self) -> None:
+        if getattr(self, "_batch", None) is not None:
+            lib().iane_gb_rl_batch_destroy(self._batch)
+            self._batch = None
 
     def __del__(self):
         try:

@@ -75,6 +75,17 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_rl_run_host.restype = ctypes.c_int
     l.iane_gb_rl_run_noalloc.argtypes = [_VIEW_P, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp]
     l.iane_gb_rl_run_noalloc.restype = ctypes.c_int
+    l.iane_gb_rl_batch_prepare.argtypes = [_VIEW_P, ctypes.c_int, i32p, ctypes.c_uint, vp, ctypes.POINTER(vp)]
+    l.iane_gb_rl_batch_prepare.restype = ctypes.c_int
+    l.iane_gb_rl_batch_scratch_bytes.argtypes = [cvp]
+    l.iane_gb_rl_batch_scratch_bytes.restype = ctypes.c_size_t
+    l.iane_gb_rl_batch_tiles.argtypes = [cvp, i32p]
+    l.iane_gb_rl_batch_tiles.restype = ctypes.c_int
+    l.iane_gb_rl_batch_run.argtypes = [vp, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp,
+                                       ctypes.c_size_t, vp]
+    l.iane_gb_rl_batch_run.restype = ctypes.c_int
+    l.iane_gb_rl_batch_destroy.argtypes = [vp]
+    l.iane_gb_rl_batch_destroy.restype = ctypes.c_int
     l.iane_gb_rl_destroy.argtypes = [vp]
     l.iane_gb_rl_destroy.restype = ctypes.c_int
     if l.iane_gb_abi_version() != abi.ABI_VERSION:

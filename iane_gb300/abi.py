@@ -23,6 +23,7 @@ ACC_FAST, ACC_EXACT = 0, 1
 
 RL_INIT_OBSERVED, RL_INIT_MEAN, RL_INIT_GIVEN = 0, 1, 2
 RL_BF16_TENSOR = 1
+BATCH_AUTOTUNE = 1
 
 OK = 0
 INVALID_ARGUMENT = -1

@@ -73,9 +73,14 @@ inline size_t tile_smem_bytes(int ky, int kz)
 	return 2 * plane + 2 * psf + 16;
 }
 
+// One output tile (x0, y0, z) of the tiled convolution. Persistent kernels call it once per
+// work item; `phases` carries the parity of the next wait on each tile buffer's mbarrier
+// (bit b for buffer b) from one call to the next, and `bars` are initialised by the caller.
+// The epilogue's row() runs here; its finish() is the caller's. `bars` are the two tile
+// mbarriers (TMA path), initialised by the caller.
 template<int KX, int WX, int WY, bool TMA, class Epi>
-__global__ void __launch_bounds__(32 * WX * WY)
-	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const Epi epi_in)
+__device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, const TileArgs& a, Epi& epi, int x0,
+	int y0, int z, uint32_t& phases, uint64_t* bars)
 {
 	using G = TileGeom<KX>;
 	constexpr int TX = 32 * WX;
@@ -92,13 +97,11 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	float* tiles = reinterpret_cast<float*>(smem_raw);
 	float* psf_s = tiles + 2 * plane_floats; // taps of two kernel planes
 	const int psf_floats = ((ky * G::KXP + 31) & ~31);
-	uint64_t* bars = reinterpret_cast<uint64_t*>(psf_s + 2 * psf_floats);
 
 	const int tid = threadIdx.x;
 	const int lane = tid & 31, warp = tid >> 5;
 	const int tx_b = (warp % WX) * 4 + (lane & 3);
 	const int ty_b = (warp / WX) * 8 + (lane >> 2);
-	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
 
 	// Kernel planes that touch the image: all of them except, for a zero border, planes
 	// whose input plane lies outside (those contribute only zero samples).
@@ -125,22 +128,17 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	};
 	if (nplanes > 0) load_taps(0);
 	if (nplanes > 1) load_taps(1);
-	if constexpr (TMA) {
-		if (tid == 0) {
-			mbar_init(&bars[0], 1);
-			mbar_init(&bars[1], 1);
-			fence_barrier_init();
-		}
-	}
-	__syncthreads();
+	__syncthreads(); // taps visible; every lane is done with the previous tile's buffers
 
 	auto issue = [&](int p) {
 		float* dst = tiles + (p & 1) * plane_floats;
 		const int qz = qz_lo + p;
 		if constexpr (TMA) {
 			if (tid == 0) {
+				// order earlier generic-proxy use of this buffer before the async-proxy write
+				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 				mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(P * H * 4));
-				tma_load_3d(dst, &tmap, x0 - G::RXA, y0 - ry, z + rz - qz, &bars[p & 1]);
+				tma_load_3d(dst, tmap_ptr, x0 - G::RXA, y0 - ry, z + rz - qz, &bars[p & 1]);
 			}
 		} else {
 			int zi = 0;
@@ -169,10 +167,12 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	if (nplanes > 1) issue(1);
 	for (int p = 0; p < nplanes; ++p) {
 		if constexpr (TMA) {
-			if (ok && !mbar_wait_bounded(&bars[p & 1], (p >> 1) & 1)) {
+			const uint32_t bit = 1u << (p & 1);
+			if (ok && !mbar_wait_bounded(&bars[p & 1], (phases & bit) ? 1u : 0u)) {
 				ok = false;
 				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
+			phases ^= bit;
 		} else {
 			if (p + 1 < nplanes) {
 				cp_async_wait<1>();
@@ -238,13 +238,41 @@ __global__ void __launch_bounds__(32 * WX * WY)
 		}
 	}
 
-	Epi epi = epi_in;
 	const int xo = x0 + kRX * tx_b;
 	const int yo = y0 + kRY * ty_b;
 #pragma unroll
 	for (int j = 0; j < kRY; ++j) {
 		epi.row(xo, yo + j, z, acc[j]);
 	}
+}
+
+// Shared memory bytes of the tile barriers (after the tiles and taps of conv_tile_body).
+template<int KX, int WX, int WY>
+__device__ __forceinline__ uint64_t* tile_barriers(int ky)
+{
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	const int H = 32 * WY + 2 * (ky / 2);
+	const int plane_floats = ((TileWidth<KX, WX>::P * H + 31) & ~31);
+	const int psf_floats = ((ky * TileGeom<KX>::KXP + 31) & ~31);
+	return reinterpret_cast<uint64_t*>(reinterpret_cast<float*>(smem_raw) + 2 * plane_floats + 2 * psf_floats);
+}
+
+template<int KX, int WX, int WY, bool TMA, class Epi>
+__global__ void __launch_bounds__(32 * WX * WY)
+	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const Epi epi_in)
+{
+	if constexpr (TMA) {
+		if (threadIdx.x == 0) {
+			uint64_t* bars = tile_barriers<KX, WX, WY>(a.ky);
+			mbar_init(&bars[0], 1);
+			mbar_init(&bars[1], 1);
+			fence_barrier_init();
+		}
+	}
+	Epi epi = epi_in;
+	uint32_t phases = 0;
+	conv_tile_body<KX, WX, WY, TMA, Epi>(&tmap, a, epi, blockIdx.x * 32 * WX, blockIdx.y * 32 * WY, blockIdx.z, phases,
+		tile_barriers<KX, WX, WY>(a.ky));
 	epi.finish();
 }
 

@@ -13,6 +13,7 @@
 #include "kernels.h"
 #include "rl.cuh"
 #include "rl_tc.cuh"
+#include "rl_batch.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -210,6 +211,51 @@ bool is_work_layout(const DevView& v, long long pitch)
 }
 
 }  // namespace
+}  // namespace iane_gb
+
+namespace iane_gb {
+
+void rl_plan_fill_passes(const iane_gb_rl_plan* plan, TileArgs* pa, TileArgs* pb, EpiRatio* ea, EpiUpdate* eb,
+	int* status)
+{
+	TileArgs t{};
+	t.nx = plan->ext[0];
+	t.ny = plan->ext[1];
+	t.nz = plan->ext[2];
+	t.ky = plan->k[1];
+	t.kz = plan->k[2];
+	t.k_stride[0] = 4;
+	t.k_stride[1] = 4LL * plan->k[0];
+	t.k_stride[2] = 4LL * plan->k[0] * plan->k[1];
+	t.border = IANE_GB_BORDER_ZERO;
+	t.status = status;
+	*pa = t;
+	*pb = t;
+	pa->kernel = reinterpret_cast<const char*>(plan->d_psf);
+	pb->kernel = reinterpret_cast<const char*>(plan->d_adj);
+	const long long plane = plan->pitch * plan->ext[1];
+	*ea = EpiRatio{};
+	ea->pitch = plan->pitch;
+	ea->plane = plane;
+	ea->nx = plan->ext[0];
+	ea->ny = plan->ext[1];
+	*eb = EpiUpdate{};
+	eb->pitch = plan->pitch;
+	eb->plane = plane;
+	eb->nx = plan->ext[0];
+	eb->ny = plan->ext[1];
+	eb->nz = plan->ext[2];
+	eb->cls = plan->d_cls;
+	eb->sens = plan->d_sens;
+	eb->cx_count = plan->ccount[0];
+	eb->cy_count = plan->ccount[1];
+	for (int i = 0; i < 3; ++i) {
+		eb->ilo[i] = plan->ilo[i];
+		eb->ihi[i] = plan->ihi[i];
+	}
+	eb->s_interior = plan->s_interior;
+}
+
 }  // namespace iane_gb
 
 // ------------------------------------------------------------------------------------

@@ -1,0 +1,76 @@
+// The persistent batch-pass kernel template (instantiated once per tile shape and pass in
+// rl_batch_k*.cu so that the variants compile in parallel).
+#pragma once
+
+#include "rl_batch.cuh"
+
+namespace iane_gb {
+
+// Bytes after the largest tiles/taps of a launch: the two tile mbarriers and the work item.
+constexpr size_t kBatchTail = 32;
+
+template<int WX, bool PASS_B, class Epi>
+__device__ __forceinline__ void batch_run_item(const BatchImage& im, Epi& epi, int x0, int y0, uint32_t& phases,
+	uint64_t* bars)
+{
+	const CUtensorMap* map = PASS_B ? &im.map_ratio : &im.map_est;
+	const TileArgs& a = PASS_B ? im.pass_b : im.pass_a;
+	switch (im.kx) {
+#define IANE_GB_BATCH_KX(K) \
+	case K: conv_tile_body<K, WX, WX, true, Epi>(map, a, epi, x0, y0, 0, phases, bars); break;
+	IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
+	IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
+	IANE_GB_BATCH_KX(17) IANE_GB_BATCH_KX(19) IANE_GB_BATCH_KX(21) IANE_GB_BATCH_KX(23)
+	IANE_GB_BATCH_KX(25) IANE_GB_BATCH_KX(27) IANE_GB_BATCH_KX(29) IANE_GB_BATCH_KX(31)
+#undef IANE_GB_BATCH_KX
+	default: break;
+	}
+}
+
+// total = dynamic shared memory of the launch: the largest tiles/taps + kBatchTail.
+template<int WX, bool PASS_B>
+__global__ void __launch_bounds__(32 * WX * WX) batch_pass_kernel(const BatchImage* __restrict__ images,
+	const BatchItem* __restrict__ items, int count, unsigned int* counter, int last, unsigned int total)
+{
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + total - kBatchTail);
+	int* item_s = reinterpret_cast<int*>(smem_raw + total - kBatchTail + 16);
+	if (threadIdx.x == 0) {
+		mbar_init(&bars[0], 1);
+		mbar_init(&bars[1], 1);
+		fence_barrier_init();
+	}
+	uint32_t phases = 0;
+	for (;;) {
+		__syncthreads(); // the previous item is finished everywhere; barriers initialised
+		if (threadIdx.x == 0) {
+			*item_s = static_cast<int>(atomicAdd(counter, 1u));
+		}
+		__syncthreads();
+		const int it = *item_s;
+		if (it >= count) {
+			break;
+		}
+		const BatchItem w = items[it];
+		const BatchImage& im = images[w.image];
+		const int x0 = (w.tile % im.tiles_x) * 32 * WX;
+		const int y0 = (w.tile / im.tiles_x) * 32 * WX;
+		if constexpr (PASS_B) {
+			EpiUpdate epi = im.epi_b;
+			epi.write_out = last && im.write_out_final;
+			batch_run_item<WX, true>(im, epi, x0, y0, phases, bars);
+		} else {
+			EpiRatio epi = im.epi_a;
+			batch_run_item<WX, false>(im, epi, x0, y0, phases, bars);
+		}
+	}
+}
+
+template<int WX, bool PASS_B>
+int launch_batch_kernel(const BatchImage* images, const BatchItem* items, int count, unsigned int* counter, int last,
+	int grid, size_t total, cudaStream_t stream);
+
+template<int WX>
+const void* batch_kernel_handle_impl();
+
+}  // namespace iane_gb

@@ -72,3 +72,30 @@ def rl_volume_workload_bf16(seed=0):
     psf = gaussian_psf((9, 9, 9), (2.5, 2.5, 2.5))
     observed = poisson(blur_zero_border(truth, psf), seed=seed + 1)
     return observed, psf, truth
+
+
+def batch_workload(count=256, seed=0, side=(64, 1024)):
+    """Uneven 2-D batch: sides log-uniform in `side` (independently, so non-square), each
+    image sparse point sources (0.2% of pixels, intensities 200-5000) on a smooth background
+    (two broad Gaussian bumps, 5-40 counts), with its own normalised Gaussian PSF of odd
+    size 3-31 and sigma 0.5-5. Returns (truths, psfs) as lists of C-ordered float32 arrays;
+    blur and noise are applied by the caller (on the GPU in bench.py)."""
+    rng = np.random.default_rng(seed)
+    truths, psfs = [], []
+    lo, hi = np.log(side[0]), np.log(side[1])
+    for _ in range(count):
+        nx = int(round(np.exp(rng.uniform(lo, hi))))
+        ny = int(round(np.exp(rng.uniform(lo, hi))))
+        yy, xx = np.meshgrid(np.arange(ny, dtype=np.float32), np.arange(nx, dtype=np.float32), indexing="ij")
+        img = np.zeros((ny, nx), np.float32)
+        for _b in range(2):
+            cx, cy = rng.uniform(0, nx), rng.uniform(0, ny)
+            s = rng.uniform(0.2, 0.6) * max(nx, ny)
+            img += np.float32(rng.uniform(5, 40)) * np.exp(-((xx - cx) ** 2 + (yy - cy) ** 2) / (2 * s * s))
+        npts = max(1, int(0.002 * nx * ny))
+        img[rng.integers(0, ny, npts), rng.integers(0, nx, npts)] += rng.uniform(200, 5000, npts).astype(np.float32)
+        k = int(rng.integers(1, 16)) * 2 + 1
+        sigma = float(rng.uniform(0.5, 5.0))
+        truths.append(img)
+        psfs.append(gaussian_psf((k, k), (sigma, sigma)))
+    return truths, psfs

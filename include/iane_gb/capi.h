@@ -179,6 +179,31 @@ int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int ob
 int iane_gb_rl_destroy(iane_gb_rl_plan* plan);
 
 /*
+ * Batched Richardson-Lucy over many 2-D images of uneven size, each with its own PSF. No
+ * counterpart in the reference (its example runs one image per process). Each pass of every
+ * iteration is one persistent launch per tile shape over a device work queue of
+ * (image, tile) items; the whole schedule is captured into a CUDA graph on the first run
+ * and replayed while the views, scratch and parameters stay the same.
+ * psfs: `count` f32 2-D device views (odd extents up to 31 x 63); extents: 2*count ints
+ * (nx, ny per image). IANE_GB_BATCH_AUTOTUNE times 32x32 against 64x64 tiles per
+ * (image shape, PSF size, dtype, SM count) and caches the choice in the file named by the
+ * environment variable IANE_GB_TUNE_CACHE (default $HOME/.cache/iane_gb300_tune.txt).
+ */
+typedef struct iane_gb_rl_batch iane_gb_rl_batch;
+#define IANE_GB_BATCH_AUTOTUNE 1u
+
+int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t* extents,
+	unsigned flags, void* stream, iane_gb_rl_batch** batch);
+size_t iane_gb_rl_batch_scratch_bytes(const iane_gb_rl_batch* batch);
+/* Tile width (32 or 64) chosen for every image. */
+int iane_gb_rl_batch_tiles(const iane_gb_rl_batch* batch, int32_t* tile_width);
+/* observed / estimates: `count` views each (observed f32 or u8, estimate f32 or u8). */
+int iane_gb_rl_batch_run(iane_gb_rl_batch* batch, const iane_gb_view* observed,
+	const iane_gb_view* estimates, int iterations, float epsilon, int init, void* scratch,
+	size_t scratch_bytes, void* stream);
+int iane_gb_rl_batch_destroy(iane_gb_rl_batch* batch);
+
+/*
  * Allocation-free Richardson-Lucy. No counterpart in the reference.
  *
  * For callers that must not allocate device memory: code recorded into a CUDA graph under
