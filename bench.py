@@ -305,7 +305,7 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30):
     torch.cuda.synchronize(dev)
     ms = a.elapsed_time(b) / reps
     pixels = sum(o.numel() for o in obs)
-    macs = sum(o.numel() * p.numel() for o, p in zip(obs, psfs)) * 2 * iterations
+    macs = sum(o.numel() * p.size for o, p in zip(obs, psfs)) * 2 * iterations
     widths = batch.tile_widths()
     batch.close()
     assert all(bool(torch.isfinite(o).all()) for o in outs)
