@@ -86,6 +86,20 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_rl_batch_run.restype = ctypes.c_int
     l.iane_gb_rl_batch_destroy.argtypes = [vp]
     l.iane_gb_rl_batch_destroy.restype = ctypes.c_int
+    sz, ll, f, i = ctypes.c_size_t, ctypes.c_longlong, ctypes.c_float, ctypes.c_int
+    l.iane_gb_cnn_conv3.argtypes = [vp, i, vp, i, i, i, i, vp, vp, i, vp, vp, vp, i, vp, vp]
+    l.iane_gb_cnn_wgrad_scratch_bytes.argtypes = [i, i, i, i, i, i]
+    l.iane_gb_cnn_wgrad_scratch_bytes.restype = sz
+    l.iane_gb_cnn_conv3_wgrad.argtypes = [vp, i, vp, i, i, i, i, vp, i, vp, vp, vp, sz, vp]
+    l.iane_gb_cnn_flip.argtypes = [vp, i, i, vp, vp]
+    l.iane_gb_cnn_pool2.argtypes = [vp, i, i, i, i, vp, vp]
+    l.iane_gb_cnn_pool2_grad.argtypes = [vp, i, i, i, i, vp, vp, i, vp]
+    l.iane_gb_cnn_up2.argtypes = [vp, i, i, i, i, vp, vp]
+    l.iane_gb_cnn_up2_grad.argtypes = [vp, i, i, i, i, vp, vp, vp]
+    l.iane_gb_cnn_mse.argtypes = [vp, vp, ll, vp, vp, vp]
+    l.iane_gb_cnn_adam.argtypes = [vp, vp, vp, vp, vp, ll, f, f, f, f, i, f, vp]
+    for name in ("conv3", "conv3_wgrad", "flip", "pool2", "pool2_grad", "up2", "up2_grad", "mse", "adam"):
+        getattr(l, "iane_gb_cnn_" + name).restype = ctypes.c_int
     l.iane_gb_rl_destroy.argtypes = [vp]
     l.iane_gb_rl_destroy.restype = ctypes.c_int
     if l.iane_gb_abi_version() != abi.ABI_VERSION:
