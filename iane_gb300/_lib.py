@@ -98,7 +98,12 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_cnn_up2_grad.argtypes = [vp, i, i, i, i, vp, vp, vp]
     l.iane_gb_cnn_mse.argtypes = [vp, vp, ll, vp, vp, vp]
     l.iane_gb_cnn_adam.argtypes = [vp, vp, vp, vp, vp, ll, f, f, f, f, i, f, vp]
-    for name in ("conv3", "conv3_wgrad", "flip", "pool2", "pool2_grad", "up2", "up2_grad", "mse", "adam"):
+    l.iane_gb_cnn_tc_packed_bytes.argtypes = [i, i, i]
+    l.iane_gb_cnn_tc_packed_bytes.restype = sz
+    l.iane_gb_cnn_tc_pack.argtypes = [vp, i, i, i, vp, vp]
+    l.iane_gb_cnn_conv3_tc.argtypes = [vp, i, vp, i, i, i, i, vp, vp, i, vp, vp, vp, i, vp]
+    for name in ("conv3", "conv3_wgrad", "flip", "pool2", "pool2_grad", "up2", "up2_grad", "mse", "adam", "tc_pack",
+                 "conv3_tc"):
         getattr(l, "iane_gb_cnn_" + name).restype = ctypes.c_int
     l.iane_gb_rl_destroy.argtypes = [vp]
     l.iane_gb_rl_destroy.restype = ctypes.c_int

@@ -119,6 +119,15 @@ int encode_tensor_map_f32(CUtensorMap* map, const void* base, int nx, int ny, in
 int encode_tensor_map(CUtensorMap* map, int data_type, const void* base, int nx, int ny, int nz, long long row_pitch,
 	long long plane_pitch, int bx, int by)
 {
+	const long long dims[3] = {nx, ny, nz};
+	const long long strides[2] = {row_pitch, plane_pitch};
+	const int box[3] = {bx, by, 1};
+	return encode_tensor_map_nd(map, data_type, 3, base, dims, strides, box);
+}
+
+int encode_tensor_map_nd(CUtensorMap* map, int data_type, int rank, const void* base, const long long* dims_in,
+	const long long* byte_strides, const int* box_in)
+{
 	using encode_fn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
 		const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
 		CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -136,12 +145,17 @@ int encode_tensor_map(CUtensorMap* map, int data_type, const void* base, int nx,
 	if (!encode) {
 		return fail(IANE_GB_CUDA_ERROR, "cuTensorMapEncodeTiled is not available from the driver");
 	}
-	const cuuint64_t dims[3] = {static_cast<cuuint64_t>(nx), static_cast<cuuint64_t>(ny), static_cast<cuuint64_t>(nz)};
-	const cuuint64_t strides[2] = {static_cast<cuuint64_t>(row_pitch), static_cast<cuuint64_t>(plane_pitch)};
-	const cuuint32_t box[3] = {static_cast<cuuint32_t>(bx), static_cast<cuuint32_t>(by), 1};
-	const cuuint32_t estride[3] = {1, 1, 1};
-	const CUresult r = encode(map, static_cast<CUtensorMapDataType>(data_type), 3, const_cast<void*>(base), dims, strides, box,
-		estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+	if (rank < 1 || rank > 5) return fail(IANE_GB_INVALID_ARGUMENT, "tensor map rank must be 1..5");
+	cuuint64_t dims[5], strides[4];
+	cuuint32_t box[5], estride[5];
+	for (int i = 0; i < rank; ++i) {
+		dims[i] = static_cast<cuuint64_t>(dims_in[i]);
+		box[i] = static_cast<cuuint32_t>(box_in[i]);
+		estride[i] = 1;
+		if (i > 0) strides[i - 1] = static_cast<cuuint64_t>(byte_strides[i - 1]);
+	}
+	const CUresult r = encode(map, static_cast<CUtensorMapDataType>(data_type), static_cast<cuuint32_t>(rank),
+		const_cast<void*>(base), dims, strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
 		CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	if (r != CUDA_SUCCESS) {
 		return fail(IANE_GB_CUDA_ERROR, "cuTensorMapEncodeTiled failed with code " + std::to_string(static_cast<int>(r)));

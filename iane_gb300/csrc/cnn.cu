@@ -1,5 +1,12 @@
-// Kernels of the learned warm start: a small 3-D encoder-decoder CNN over planar volumes
-// ([channel][z][y][x], x fastest), BF16 activations and weights, FP32 accumulation.
+// Kernels of the learned warm start: a small 3-D encoder-decoder CNN, BF16 activations and
+// weights, FP32 accumulation.
+//
+// Activation layout ("C8"): channels in octets, each octet voxel-major with its 8 channels
+// contiguous -- element (c, v) of a C-channel volume of V voxels sits at
+// ((c / 8) * V + v) * 8 + c % 8 (ceil(C / 8) octets; unused slots of the last octet are
+// never read as data). A voxel's octet is one 16-byte vector: the tensor-core kernel
+// (cnn_tc.cu) takes it as a row of its K-major operand straight from a TMA box. FP32
+// outputs (the network output, test readbacks) are planar [c][v].
 //
 //   conv3       y[co] = act(b[co] + sum_{ci,t} w[co][ci][t] * x[ci](v + t - 1) (+ residual)),
 //               zero padding, inputs given as two tensors concatenated along channels (the
@@ -11,10 +18,10 @@
 //               the convolution of the output gradient with these weights
 //   pool2 / up2 and their gradients, mse (loss and gradient), adam (FP32 master weights)
 //
-// Direct SIMT implementation: a CTA computes an 8x8x4 brick of output voxels for all output
-// channels, one voxel per thread with CO accumulators; input halo bricks and the weights of
-// four input channels are staged in shared memory per step, weights read as warp-uniform
-// 128-bit broadcasts.
+// Direct SIMT implementation (training and input gradients): a CTA computes an 8x8x4 brick
+// of output voxels for all output channels, one voxel per thread with CO accumulators; input
+// halo bricks and the weights of four input channels are staged in shared memory per step,
+// weights read as warp-uniform 128-bit broadcasts.
 #include "common.cuh"
 
 #include <cstdint>
@@ -29,6 +36,12 @@ constexpr int CI_STEP = 4;
 constexpr int NT = BX * BY * BZ;             // 256 threads
 
 __device__ __forceinline__ float bf(uint16_t v) { return __uint_as_float(static_cast<uint32_t>(v) << 16); }
+
+// Offset of element (c, v) in a C8 tensor of `vol` voxels.
+__host__ __device__ __forceinline__ long long c8(int c, long long v, long long vol)
+{
+	return ((static_cast<long long>(c >> 3) * vol + v) << 3) + (c & 7);
+}
 __device__ __forceinline__ uint16_t to_bf(float f)
 {
 	const __nv_bfloat16 b = __float2bfloat16_rn(f);
@@ -43,11 +56,11 @@ struct Conv3Args {
 	const uint16_t* wt;     // [co][c0 + c1][27]
 	const float* bias;      // [co] or null
 	int co;
-	uint16_t* y16;          // bf16 output, or null
-	float* y32;             // f32 output, or null
+	uint16_t* y16;          // bf16 output (C8), or null
+	float* y32;             // f32 output (planar [co][v]), or null
 	const float* residual;  // f32, added before the activation (co == 1 only), or null
 	int act;                // 0 none, 1 relu
-	const uint16_t* mask;   // [co] channels, y *= (mask > 0), or null
+	const uint16_t* mask;   // C8, co channels: y *= (mask > 0), or null
 	int bricks_x, bricks_y;
 };
 
@@ -71,14 +84,14 @@ __global__ void __launch_bounds__(NT) conv3_kernel(const Conv3Args a)
 	for (int ci0 = 0; ci0 < ci_total; ci0 += CI_STEP) {
 		__syncthreads();
 		for (int i = tid; i < CI_STEP * HALO; i += NT) {
-			const int k = i / HALO, r = i % HALO;
+			const int k = i % CI_STEP, r = i / CI_STEP;  // 4 neighbouring threads: 8 contiguous bytes
 			const int hx = r % HX, hy = (r / HX) % HY, hz = r / (HX * HY);
 			const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
 			const int ci = ci0 + k;
 			float v = 0.0f;
 			if (ci < ci_total && gx >= 0 && gx < a.w && gy >= 0 && gy < a.h && gz >= 0 && gz < a.d) {
-				const uint16_t* src = ci < a.c0 ? a.x0 + ci * vol : a.x1 + (ci - a.c0) * vol;
-				v = bf(src[gz * plane + static_cast<long long>(gy) * a.w + gx]);
+				const long long at = gz * plane + static_cast<long long>(gy) * a.w + gx;
+				v = bf(ci < a.c0 ? a.x0[c8(ci, at, vol)] : a.x1[c8(ci - a.c0, at, vol)]);
 			}
 			xs[k][r] = v;
 		}
@@ -120,14 +133,16 @@ __global__ void __launch_bounds__(NT) conv3_kernel(const Conv3Args a)
 		float v = acc[c] + (a.bias ? a.bias[c] : 0.0f);
 		if (a.residual) v += a.residual[c * vol + at];
 		if (a.act == 1) v = v > 0.0f ? v : 0.0f;
-		if (a.mask && !(bf(a.mask[c * vol + at]) > 0.0f)) v = 0.0f;
+		if (a.mask && !(bf(a.mask[c8(c, at, vol)]) > 0.0f)) v = 0.0f;
 		if (a.y32) a.y32[c * vol + at] = v;
-		if (a.y16) a.y16[c * vol + at] = to_bf(v);
+		if (a.y16) a.y16[c8(c, at, vol)] = to_bf(v);
 	}
 }
 
-// Split-K weight gradient: CTA (co tile of 16, input channel ci, voxel chunk) accumulates, for
-// each of its (output channel, tap) pairs, sum over the chunk's voxels of dy * x(shifted).
+// Split-K weight gradient: CTA (co tile of 16, input octet, voxel chunk) accumulates, for
+// each of its (output channel, tap) pairs and the octet's 8 input channels, the sum over the
+// chunk's voxels of dy * x(shifted). The octet's halo brick arrives as one 16-byte vector per
+// voxel.
 constexpr int WG_CO = 16;
 constexpr int WG_THREADS = 448; // >= 16 * 27 pairs, 14 warps
 
@@ -146,20 +161,23 @@ struct WgradArgs {
 
 __global__ void __launch_bounds__(WG_THREADS) conv3_wgrad_kernel(const WgradArgs a)
 {
-	__shared__ float xs[HALO];
+	__shared__ float xs[8][HALO];
 	__shared__ float gs[WG_CO][NT + 1];
 	const int tid = threadIdx.x;
 	const int co0 = blockIdx.x * WG_CO;
-	const int ci = blockIdx.y;
+	const int ci0 = blockIdx.y * 8;          // this CTA's input octet
 	const int chunk = blockIdx.z;
 	const int ci_total = a.c0 + a.c1;
 	const long long plane = static_cast<long long>(a.h) * a.w;
 	const long long vol = plane * a.d;
-	const int pc = tid / 27, pt = tid % 27;       // this thread's (output channel, tap)
+	const int pc = tid / 27, pt = tid % 27;  // this thread's (output channel, tap)
 	const bool active = tid < WG_CO * 27 && co0 + pc < a.co;
 	const int tx = pt % 3, ty = (pt / 3) % 3, tz = pt / 9;
-	float acc = 0.0f, bacc = 0.0f;
-	const uint16_t* xsrc = ci < a.c0 ? a.x0 + ci * vol : a.x1 + (ci - a.c0) * vol;
+	float acc[8], bacc = 0.0f;
+#pragma unroll
+	for (int k = 0; k < 8; ++k) acc[k] = 0.0f;
+	// the octet lies in one input tensor (c0 is a multiple of 8 or the only tensor)
+	const uint16_t* xsrc = ci0 < a.c0 ? a.x0 + c8(ci0, 0, vol) : a.x1 + c8(ci0 - a.c0, 0, vol);
 	const int b_begin = chunk * a.chunk_bricks;
 	const int b_end = min(a.bricks_total, b_begin + a.chunk_bricks);
 	for (int b = b_begin; b < b_end; ++b) {
@@ -169,37 +187,50 @@ __global__ void __launch_bounds__(WG_THREADS) conv3_wgrad_kernel(const WgradArgs
 		for (int i = tid; i < HALO; i += WG_THREADS) {
 			const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
 			const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
-			float v = 0.0f;
+			uint4 q = make_uint4(0u, 0u, 0u, 0u);
 			if (gx >= 0 && gx < a.w && gy >= 0 && gy < a.h && gz >= 0 && gz < a.d) {
-				v = bf(xsrc[gz * plane + static_cast<long long>(gy) * a.w + gx]);
+				q = *reinterpret_cast<const uint4*>(xsrc + ((gz * plane + static_cast<long long>(gy) * a.w + gx) << 3));
 			}
-			xs[i] = v;
+			const uint32_t wv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+			for (int k = 0; k < 4; ++k) {
+				xs[2 * k][i] = __uint_as_float(wv[k] << 16);
+				xs[2 * k + 1][i] = __uint_as_float(wv[k] & 0xFFFF0000u);
+			}
 		}
 		for (int i = tid; i < WG_CO * NT; i += WG_THREADS) {
-			const int c = i / NT, r = i % NT;
+			const int c = i % WG_CO, r = i / WG_CO;  // 16 neighbouring threads: one voxel's channels
 			const int lx = r % BX, ly = (r / BX) % BY, lz = r / (BX * BY);
 			const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
 			float v = 0.0f;
 			if (co0 + c < a.co && gx < a.w && gy < a.h && gz < a.d) {
-				v = bf(a.dy[(co0 + c) * vol + gz * plane + static_cast<long long>(gy) * a.w + gx]);
+				v = bf(a.dy[c8(co0 + c, gz * plane + static_cast<long long>(gy) * a.w + gx, vol)]);
 			}
 			gs[c][r] = v;
 		}
 		__syncthreads();
 		if (active) {
 			const float* g = gs[pc];
-#pragma unroll 4
+#pragma unroll 2
 			for (int r = 0; r < NT; ++r) {
 				const int lx = r % BX, ly = (r / BX) % BY, lz = r / (BX * BY);
-				acc = fmaf(g[r], xs[(lz + tz) * HX * HY + (ly + ty) * HX + lx + tx], acc);
-				if (pt == 0) bacc += g[r];
+				const int at = (lz + tz) * HX * HY + (ly + ty) * HX + lx + tx;
+				const float gv = g[r];
+#pragma unroll
+				for (int k = 0; k < 8; ++k) acc[k] = fmaf(gv, xs[k][at], acc[k]);
+				bacc += gv;
 			}
 		}
 	}
 	if (active) {
-		const long long idx = ((static_cast<long long>(chunk) * a.co + co0 + pc) * ci_total + ci) * 27 + pt;
-		a.partial[idx] = acc;
-		if (pt == 0 && ci == 0) {
+#pragma unroll
+		for (int k = 0; k < 8; ++k) {
+			const int ci = ci0 + k;
+			if (ci < ci_total) {
+				a.partial[((static_cast<long long>(chunk) * a.co + co0 + pc) * ci_total + ci) * 27 + pt] = acc[k];
+			}
+		}
+		if (pt == 0 && ci0 == 0) {
 			a.partial[static_cast<long long>(a.chunks) * a.co * ci_total * 27 + static_cast<long long>(chunk) * a.co + co0 + pc] =
 				bacc;
 		}
@@ -237,20 +268,22 @@ __global__ void flip_kernel(const uint16_t* w, int co, int ci, uint16_t* wt)
 }
 
 // Average pooling 2x2x2 (input d, h, w even) and its gradient (optionally masked by the
-// pooled layer's input activations).
+// pooled layer's input activations). C8 tensors are indexed flat: (octet, voxel, lane).
 __global__ void pool2_kernel(const uint16_t* x, int c, int d, int h, int w, uint16_t* y)
 {
 	const int od = d / 2, oh = h / 2, ow = w / 2;
-	const long long n = static_cast<long long>(c) * od * oh * ow;
+	const long long ovol = static_cast<long long>(od) * oh * ow, ivol = static_cast<long long>(d) * h * w;
+	const long long n = static_cast<long long>((c + 7) / 8) * ovol * 8;
 	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
 	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int ox = static_cast<int>(i % ow), oy = static_cast<int>((i / ow) % oh);
-		const int oz = static_cast<int>((i / (static_cast<long long>(ow) * oh)) % od);
-		const long long ch = i / (static_cast<long long>(ow) * oh * od);
-		const uint16_t* src = x + ch * d * static_cast<long long>(h) * w;
+		const int lane = static_cast<int>(i & 7);
+		const long long ov = (i >> 3) % ovol, oct = (i >> 3) / ovol;
+		const int ox = static_cast<int>(ov % ow), oy = static_cast<int>((ov / ow) % oh), oz = static_cast<int>(ov / (static_cast<long long>(ow) * oh));
+		const uint16_t* src = x + oct * ivol * 8 + lane;
 		float s = 0.0f;
 		for (int k = 0; k < 8; ++k) {
-			s += bf(src[(2 * oz + (k >> 2)) * static_cast<long long>(h) * w + (2 * oy + ((k >> 1) & 1)) * w + 2 * ox + (k & 1)]);
+			const long long v = (2 * oz + (k >> 2)) * static_cast<long long>(h) * w + (2 * oy + ((k >> 1) & 1)) * w + 2 * ox + (k & 1);
+			s += bf(src[v * 8]);
 		}
 		y[i] = to_bf(0.125f * s);
 	}
@@ -259,14 +292,16 @@ __global__ void pool2_kernel(const uint16_t* x, int c, int d, int h, int w, uint
 __global__ void pool2_grad_kernel(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx, const uint16_t* mask,
 	int accumulate)
 {
-	const long long n = static_cast<long long>(c) * d * h * w;
+	const long long ivol = static_cast<long long>(d) * h * w;
+	const long long ovol = ivol / 8;
+	const long long n = static_cast<long long>((c + 7) / 8) * ivol * 8;
 	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
 	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int xx = static_cast<int>(i % w), yy = static_cast<int>((i / w) % h);
-		const int zz = static_cast<int>((i / (static_cast<long long>(w) * h)) % d);
-		const long long ch = i / (static_cast<long long>(w) * h * d);
-		const long long o = ((ch * (d / 2) + zz / 2) * (h / 2) + yy / 2) * (w / 2) + xx / 2;
-		float g = 0.125f * bf(dy[o]);
+		const int lane = static_cast<int>(i & 7);
+		const long long v = (i >> 3) % ivol, oct = (i >> 3) / ivol;
+		const int xx = static_cast<int>(v % w), yy = static_cast<int>((v / w) % h), zz = static_cast<int>(v / (static_cast<long long>(w) * h));
+		const long long o = (static_cast<long long>(zz / 2) * (h / 2) + yy / 2) * (w / 2) + xx / 2;
+		float g = 0.125f * bf(dy[((oct * ovol + o) << 3) + lane]);
 		if (accumulate) g += bf(dx[i]);
 		if (mask && !(bf(mask[i]) > 0.0f)) g = 0.0f;
 		dx[i] = to_bf(g);
@@ -277,35 +312,40 @@ __global__ void pool2_grad_kernel(const uint16_t* dy, int c, int d, int h, int w
 __global__ void up2_kernel(const uint16_t* x, int c, int d, int h, int w, uint16_t* y)
 {
 	const int od = 2 * d, oh = 2 * h, ow = 2 * w;
-	const long long n = static_cast<long long>(c) * od * oh * ow;
+	const long long ovol = static_cast<long long>(od) * oh * ow, ivol = static_cast<long long>(d) * h * w;
+	const long long n = static_cast<long long>((c + 7) / 8) * ovol * 8;
 	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
 	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int ox = static_cast<int>(i % ow), oy = static_cast<int>((i / ow) % oh);
-		const int oz = static_cast<int>((i / (static_cast<long long>(ow) * oh)) % od);
-		const long long ch = i / (static_cast<long long>(ow) * oh * od);
-		y[i] = x[((ch * d + oz / 2) * h + oy / 2) * w + ox / 2];
+		const int lane = static_cast<int>(i & 7);
+		const long long ov = (i >> 3) % ovol, oct = (i >> 3) / ovol;
+		const int ox = static_cast<int>(ov % ow), oy = static_cast<int>((ov / ow) % oh), oz = static_cast<int>(ov / (static_cast<long long>(ow) * oh));
+		const long long v = (static_cast<long long>(oz / 2) * h + oy / 2) * w + ox / 2;
+		y[i] = x[((oct * ivol + v) << 3) + lane];
 	}
 }
 
 __global__ void up2_grad_kernel(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx, const uint16_t* mask)
 {
-	const long long n = static_cast<long long>(c) * d * h * w;
+	const long long ivol = static_cast<long long>(d) * h * w, ovol = 8 * ivol;
+	const long long n = static_cast<long long>((c + 7) / 8) * ivol * 8;
 	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
 	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int xx = static_cast<int>(i % w), yy = static_cast<int>((i / w) % h);
-		const int zz = static_cast<int>((i / (static_cast<long long>(w) * h)) % d);
-		const long long ch = i / (static_cast<long long>(w) * h * d);
-		const uint16_t* src = dy + ch * 8 * static_cast<long long>(d) * h * w;
+		const int lane = static_cast<int>(i & 7);
+		const long long v = (i >> 3) % ivol, oct = (i >> 3) / ivol;
+		const int xx = static_cast<int>(v % w), yy = static_cast<int>((v / w) % h), zz = static_cast<int>(v / (static_cast<long long>(w) * h));
+		const uint16_t* src = dy + oct * ovol * 8 + lane;
 		float s = 0.0f;
 		for (int k = 0; k < 8; ++k) {
-			s += bf(src[(2 * zz + (k >> 2)) * 4LL * h * w + (2 * yy + ((k >> 1) & 1)) * 2LL * w + 2 * xx + (k & 1)]);
+			const long long o = (2 * zz + (k >> 2)) * 4LL * h * w + (2 * yy + ((k >> 1) & 1)) * 2LL * w + 2 * xx + (k & 1);
+			s += bf(src[o * 8]);
 		}
 		if (mask && !(bf(mask[i]) > 0.0f)) s = 0.0f;
 		dx[i] = to_bf(s);
 	}
 }
 
-// loss = sum (y - t)^2 / n (FP64 accumulation per CTA, atomically added), dy = 2 (y - t) / n.
+// loss = sum (y - t)^2 / n (FP64 accumulation per CTA, atomically added), dy = 2 (y - t) / n
+// (a one-channel C8 tensor: slot 0 of each voxel's octet).
 __global__ void mse_kernel(const float* y, const float* t, long long n, uint16_t* dy, double* loss)
 {
 	double s = 0.0;
@@ -313,7 +353,7 @@ __global__ void mse_kernel(const float* y, const float* t, long long n, uint16_t
 	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
 		const float e = y[i] - t[i];
 		s += static_cast<double>(e) * e;
-		dy[i] = to_bf(2.0f * e / static_cast<float>(n));
+		dy[i * 8] = to_bf(2.0f * e / static_cast<float>(n));  // one channel, C8 layout
 	}
 	__shared__ double red[32];
 	for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
@@ -341,6 +381,16 @@ __global__ void adam_kernel(float* p, uint16_t* p16, const float* g, float* m, f
 		p[i] -= upd;
 		if (p16) p16[i] = to_bf(p[i]);
 	}
+}
+
+// Voxel chunks of the split-K weight gradient: about four CTAs per SM in all.
+long long wgrad_chunks(int c0, int c1, int d, int h, int w, int co)
+{
+	const long long bricks = static_cast<long long>((w + BX - 1) / BX) * ((h + BY - 1) / BY) * ((d + BZ - 1) / BZ);
+	const int co_tiles = (co + WG_CO - 1) / WG_CO;
+	const int octets = (c0 + 7) / 8 + (c1 + 7) / 8;
+	long long chunks = (4LL * device_sm_count()) / (co_tiles * octets);
+	return chunks < 1 ? 1 : (chunks > bricks ? bricks : chunks);
 }
 
 int grid1(long long n)
@@ -385,18 +435,19 @@ int iane_gb_cnn_conv3(const uint16_t* x0, int c0, const uint16_t* x1, int c1, in
 
 size_t iane_gb_cnn_wgrad_scratch_bytes(int c0, int c1, int d, int h, int w, int co)
 {
-	const long long bricks = static_cast<long long>((w + BX - 1) / BX) * ((h + BY - 1) / BY) * ((d + BZ - 1) / BZ);
-	const int co_tiles = (co + WG_CO - 1) / WG_CO;
-	long long chunks = (4LL * device_sm_count()) / (co_tiles * (c0 + c1));
-	chunks = chunks < 1 ? 1 : (chunks > bricks ? bricks : chunks);
+	const long long chunks = wgrad_chunks(c0, c1, d, h, w, co);
 	return static_cast<size_t>(chunks) * co * ((c0 + c1) * 27 + 1) * sizeof(float);
 }
 
 int iane_gb_cnn_conv3_wgrad(const uint16_t* x0, int c0, const uint16_t* x1, int c1, int d, int h, int w,
 	const uint16_t* dy, int co, float* dw, float* db, void* scratch, size_t scratch_bytes, void* stream)
 {
-	if (!x0 || c0 < 1 || c1 < 0 || (c1 > 0 && !x1) || !dy || !dw || co < 1 || co > 64 || !scratch) {
+	if (!x0 || c0 < 1 || c1 < 0 || (c1 > 0 && (!x1 || c0 % 8 != 0)) || !dy || !dw || co < 1 || co > 64 || !scratch ||
+	    d < 1 || h < 1 || w < 1) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_conv3_wgrad: bad arguments");
+	}
+	if (reinterpret_cast<uintptr_t>(x0) % 16 || reinterpret_cast<uintptr_t>(x1) % 16) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_conv3_wgrad: inputs must be 16-byte aligned");
 	}
 	if (scratch_bytes < iane_gb_cnn_wgrad_scratch_bytes(c0, c1, d, h, w, co)) {
 		return fail(IANE_GB_LENGTH_ERROR, "cnn_conv3_wgrad: scratch too small");
@@ -405,8 +456,8 @@ int iane_gb_cnn_conv3_wgrad(const uint16_t* x0, int c0, const uint16_t* x1, int 
 	const long long bricks = static_cast<long long>(bx) * by * bz;
 	const int co_tiles = (co + WG_CO - 1) / WG_CO;
 	const int ci_total = c0 + c1;
-	long long chunks = (4LL * device_sm_count()) / (co_tiles * ci_total);
-	chunks = chunks < 1 ? 1 : (chunks > bricks ? bricks : chunks);
+	const int octets = (c0 + 7) / 8 + (c1 + 7) / 8;
+	const long long chunks = wgrad_chunks(c0, c1, d, h, w, co);
 	WgradArgs a{};
 	a.x0 = x0;
 	a.x1 = x1;
@@ -424,7 +475,7 @@ int iane_gb_cnn_conv3_wgrad(const uint16_t* x0, int c0, const uint16_t* x1, int 
 	a.partial = static_cast<float*>(scratch);
 	a.chunks = static_cast<int>(chunks);
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
-	conv3_wgrad_kernel<<<dim3(co_tiles, ci_total, static_cast<unsigned>(chunks)), WG_THREADS, 0, st>>>(a);
+	conv3_wgrad_kernel<<<dim3(co_tiles, octets, static_cast<unsigned>(chunks)), WG_THREADS, 0, st>>>(a);
 	const long long nw = static_cast<long long>(co) * ci_total * 27;
 	conv3_wgrad_reduce<<<grid1(nw + co), 256, 0, st>>>(a.partial, a.chunks, nw, co, dw, db);
 	IANE_GB_CUDA(cudaGetLastError(), "cnn_conv3_wgrad: launch");

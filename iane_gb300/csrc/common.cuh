@@ -208,6 +208,17 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 		: "memory");
 }
 
+// 5-D tiled TMA load into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+	uint64_t* bar)
+{
+	asm volatile(
+		"cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+		::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4),
+		"r"(smem_addr(bar))
+		: "memory");
+}
+
 // 4-byte asynchronous global->shared copy; src_bytes = 0 writes zero.
 __device__ __forceinline__ void cp_async4(void* dst, const void* src, int src_bytes)
 {
@@ -227,6 +238,9 @@ int encode_tensor_map_f32(CUtensorMap* map, const void* base, int nx, int ny, in
 // The same for any CUtensorMapDataType (e.g. CU_TENSOR_MAP_DATA_TYPE_BFLOAT16).
 int encode_tensor_map(CUtensorMap* map, int data_type, const void* base, int nx, int ny, int nz,
 	long long row_pitch, long long plane_pitch, int bx, int by);
+// Rank 1..5: dims[rank] elements, byte_strides[rank - 1] of dims 1.., box[rank] elements.
+int encode_tensor_map_nd(CUtensorMap* map, int data_type, int rank, const void* base, const long long* dims,
+	const long long* byte_strides, const int* box);
 
 int device_sm_count();
 

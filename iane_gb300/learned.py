@@ -66,6 +66,7 @@ class WarmStartNet:
         self.v = torch.zeros_like(self.master)
         self.steps = 0
         self._flipped = None
+        self._packed = None
         self._buffers = {}
 
     # -- parameter views ------------------------------------------------------------------
@@ -93,6 +94,8 @@ class WarmStartNet:
 
     # -- buffers per volume shape -----------------------------------------------------------
     def _buf(self, shape):
+        """Forward buffers for one volume shape: C8 activations (octets, D, H, W, 8), zeroed
+        so that unused octet slots hold zeros, and the FP32 output and residual."""
         key = tuple(shape)
         if key in self._buffers:
             return self._buffers[key]
@@ -100,25 +103,38 @@ class WarmStartNet:
         d, h, w = key
         if d % 4 or h % 4 or w % 4:
             raise ValueError("volume extents must be multiples of 4 (two 2x poolings)")
-        bf = dict(dtype=torch.bfloat16, device=self.device)
         s1, s2, s3 = (d, h, w), (d // 2, h // 2, w // 2), (d // 4, h // 4, w // 4)
-        b = {"x16": torch.empty((2,) + s1, **bf)}
+        b = {"x16": self._act(2, s1)}
         for name, c, s in (("e1a", 16, s1), ("e1b", 16, s1), ("p1", 16, s2), ("e2a", 32, s2), ("e2b", 32, s2),
                            ("p2", 32, s3), ("e3a", 64, s3), ("e3b", 64, s3), ("u2", 64, s2), ("d2a", 32, s2),
-                           ("d2b", 32, s2), ("u1", 32, s1), ("d1a", 16, s1), ("d1b", 16, s1),
-                           ("g_out", 1, s1), ("g16a", 16, s1), ("g16b", 16, s1), ("g_cat1", 48, s1),
-                           ("g32a", 32, s2), ("g32b", 32, s2), ("g_cat2", 96, s2), ("g64a", 64, s3),
-                           ("g64b", 64, s3), ("g_p2", 32, s3), ("g_p1", 16, s2)):
-            b[name] = torch.empty((c,) + s, **bf)
+                           ("d2b", 32, s2), ("u1", 32, s1), ("d1a", 16, s1), ("d1b", 16, s1)):
+            b[name] = self._act(c, s)
         b["out"] = torch.empty((1,) + s1, dtype=torch.float32, device=self.device)
         b["res"] = torch.empty((1,) + s1, dtype=torch.float32, device=self.device)
+        b["loss"] = torch.zeros(1, dtype=torch.float64, device=self.device)
+        self._buffers[key] = b
+        return b
+
+    def _act(self, c, s):
+        return self.torch.zeros(((c + 7) // 8,) + tuple(s) + (8,), dtype=self.torch.bfloat16, device=self.device)
+
+    def _grad_buf(self, shape):
+        """Gradient buffers (allocated on the first backward of a shape)."""
+        b = self._buf(shape)
+        if "g_out" in b:
+            return b
+        d, h, w = shape
+        s1, s2, s3 = (d, h, w), (d // 2, h // 2, w // 2), (d // 4, h // 4, w // 4)
+        for name, c, s in (("g_out", 1, s1), ("g16a", 16, s1), ("g16b", 16, s1), ("g_cat1", 48, s1),
+                           ("g32a", 32, s2), ("g32b", 32, s2), ("g_cat2", 96, s2), ("g64a", 64, s3),
+                           ("g64b", 64, s3), ("g_p2", 32, s3), ("g_p1", 16, s2)):
+            b[name] = self._act(c, s)
         need = 0
         for name, ci, co, _ in LAYERS:
             ls = {"e1": s1, "e2": s2, "e3": s3, "d2": s2, "d1": s1, "he": s1}[name[:2]]
-            need = max(need, lib().iane_gb_cnn_wgrad_scratch_bytes(ci, 0, *ls, co))
-        b["wg"] = torch.empty(int(need) + 256, dtype=torch.uint8, device=self.device)
-        b["loss"] = torch.zeros(1, dtype=torch.float64, device=self.device)
-        self._buffers[key] = b
+            c0, c1 = {"d2a": (64, 32), "d1a": (32, 16)}.get(name, (ci, 0))
+            need = max(need, lib().iane_gb_cnn_wgrad_scratch_bytes(c0, c1, *ls, co))
+        b["wg"] = self.torch.empty(int(need) + 256, dtype=self.torch.uint8, device=self.device)
         return b
 
     # -- operations ---------------------------------------------------------------------------
@@ -144,40 +160,65 @@ class WarmStartNet:
                 self._flipped[name] = out
         return self._flipped
 
-    def forward(self, observed_norm, sigma: float):
+    def _packs(self):
+        """Weights packed for the tensor-core forward (refreshed after each update)."""
+        if self._packed is None:
+            torch = self.torch
+            self._packed = {}
+            for name, ci, co, _ in LAYERS:
+                c0, c1 = {"d2a": (64, 32), "d1a": (32, 16)}.get(name, (ci, 0))
+                out = torch.empty(int(lib().iane_gb_cnn_tc_packed_bytes(co, c0, c1)) // 2, dtype=torch.bfloat16,
+                                  device=self.device)
+                check(lib().iane_gb_cnn_tc_pack(_p(self.w16(name)), co, c0, c1, _p(out), self._stream()))
+                self._packed[name] = out
+        return self._packed
+
+    def forward(self, observed_norm, sigma: float, tensor_cores: bool = False):
         """observed_norm: f32 tensor (D, H, W) = observed / mean(observed). Returns the
-        (1, D, H, W) f32 output (normalised estimate); activations stay for backward()."""
+        (1, D, H, W) f32 output (normalised estimate); activations stay for backward().
+        tensor_cores=True runs every convolution on the tcgen05 kernel (inference); the
+        default SIMT kernels are the ones the backward pass mirrors."""
         shape = tuple(observed_norm.shape)
         b = self._buf(shape)
         s1 = shape
         s2 = tuple(v // 2 for v in shape)
         s3 = tuple(v // 4 for v in shape)
+        st = self._stream()
         b["res"][0].copy_(observed_norm)
-        b["x16"][0].copy_(observed_norm)
-        b["x16"][1].fill_(sigma / 3.0)
-        c = self._conv
-        c(b["x16"], 2, None, 0, s1, self.w16("e1a"), self.bias("e1a"), 16, y16=b["e1a"])
-        c(b["e1a"], 16, None, 0, s1, self.w16("e1b"), self.bias("e1b"), 16, y16=b["e1b"])
-        check(lib().iane_gb_cnn_pool2(_p(b["e1b"]), 16, *s1, _p(b["p1"]), self._stream()))
-        c(b["p1"], 16, None, 0, s2, self.w16("e2a"), self.bias("e2a"), 32, y16=b["e2a"])
-        c(b["e2a"], 32, None, 0, s2, self.w16("e2b"), self.bias("e2b"), 32, y16=b["e2b"])
-        check(lib().iane_gb_cnn_pool2(_p(b["e2b"]), 32, *s2, _p(b["p2"]), self._stream()))
-        c(b["p2"], 32, None, 0, s3, self.w16("e3a"), self.bias("e3a"), 64, y16=b["e3a"])
-        c(b["e3a"], 64, None, 0, s3, self.w16("e3b"), self.bias("e3b"), 64, y16=b["e3b"])
-        check(lib().iane_gb_cnn_up2(_p(b["e3b"]), 64, *s3, _p(b["u2"]), self._stream()))
-        c(b["u2"], 64, b["e2b"], 32, s2, self.w16("d2a"), self.bias("d2a"), 32, y16=b["d2a"])
-        c(b["d2a"], 32, None, 0, s2, self.w16("d2b"), self.bias("d2b"), 32, y16=b["d2b"])
-        check(lib().iane_gb_cnn_up2(_p(b["d2b"]), 32, *s2, _p(b["u1"]), self._stream()))
-        c(b["u1"], 32, b["e1b"], 16, s1, self.w16("d1a"), self.bias("d1a"), 16, y16=b["d1a"])
-        c(b["d1a"], 16, None, 0, s1, self.w16("d1b"), self.bias("d1b"), 16, y16=b["d1b"])
-        c(b["d1b"], 16, None, 0, s1, self.w16("head"), self.bias("head"), 1, y32=b["out"], residual=b["res"],
-          relu=False)
+        b["x16"][0, ..., 0].copy_(observed_norm)
+        b["x16"][0, ..., 1].fill_(sigma / 3.0)
+        packs = self._packs() if tensor_cores else None
+
+        def c(name, x0, c0, x1, c1, s, co, y16=None, y32=None, residual=None, relu=True):
+            if packs is not None:
+                check(lib().iane_gb_cnn_conv3_tc(_p(x0), c0, _p(x1), c1, s[0], s[1], s[2], _p(packs[name]),
+                                                 _p(self.bias(name)), co, _p(y16), _p(y32), _p(residual),
+                                                 1 if relu else 0, st))
+            else:
+                self._conv(x0, c0, x1, c1, s, self.w16(name), self.bias(name), co, y16=y16, y32=y32,
+                           residual=residual, relu=relu)
+
+        c("e1a", b["x16"], 2, None, 0, s1, 16, y16=b["e1a"])
+        c("e1b", b["e1a"], 16, None, 0, s1, 16, y16=b["e1b"])
+        check(lib().iane_gb_cnn_pool2(_p(b["e1b"]), 16, *s1, _p(b["p1"]), st))
+        c("e2a", b["p1"], 16, None, 0, s2, 32, y16=b["e2a"])
+        c("e2b", b["e2a"], 32, None, 0, s2, 32, y16=b["e2b"])
+        check(lib().iane_gb_cnn_pool2(_p(b["e2b"]), 32, *s2, _p(b["p2"]), st))
+        c("e3a", b["p2"], 32, None, 0, s3, 64, y16=b["e3a"])
+        c("e3b", b["e3a"], 64, None, 0, s3, 64, y16=b["e3b"])
+        check(lib().iane_gb_cnn_up2(_p(b["e3b"]), 64, *s3, _p(b["u2"]), st))
+        c("d2a", b["u2"], 64, b["e2b"], 32, s2, 32, y16=b["d2a"])
+        c("d2b", b["d2a"], 32, None, 0, s2, 32, y16=b["d2b"])
+        check(lib().iane_gb_cnn_up2(_p(b["d2b"]), 32, *s2, _p(b["u1"]), st))
+        c("d1a", b["u1"], 32, b["e1b"], 16, s1, 16, y16=b["d1a"])
+        c("d1b", b["d1a"], 16, None, 0, s1, 16, y16=b["d1b"])
+        c("head", b["d1b"], 16, None, 0, s1, 1, y32=b["out"], residual=b["res"], relu=False)
         return b["out"]
 
     def loss_and_grad(self, target_norm):
         """MSE against target_norm (D, H, W f32); writes the output gradient; returns the
         device loss tensor (accumulated until zero_grad)."""
-        b = self._buf(tuple(target_norm.shape))
+        b = self._grad_buf(tuple(target_norm.shape))
         check(lib().iane_gb_cnn_mse(_p(b["out"]), _p(target_norm), target_norm.numel(), _p(b["g_out"]), _p(b["loss"]),
                                     self._stream()))
         return b["loss"]
@@ -185,7 +226,7 @@ class WarmStartNet:
     def backward(self, shape):
         """Accumulate parameter gradients for the last forward (its output gradient set by
         loss_and_grad)."""
-        b = self._buf(shape)
+        b = self._grad_buf(tuple(shape))
         s1 = tuple(shape)
         s2 = tuple(v // 2 for v in shape)
         s3 = tuple(v // 4 for v in shape)
@@ -243,12 +284,14 @@ class WarmStartNet:
                                      ctypes.c_float(lr), ctypes.c_float(0.9), ctypes.c_float(0.999),
                                      ctypes.c_float(1e-8), self.steps, ctypes.c_float(grad_scale), self._stream()))
         self._flipped = None
+        self._packed = None
 
     # -- warm start ---------------------------------------------------------------------------
     def warm_start(self, observed, sigma: float, epsilon: float = 1e-6):
-        """RL start for `observed` (f32 CUDA tensor, extents multiples of 4): mean * max(net, 1e-3)."""
+        """RL start for `observed` (f32 CUDA tensor, extents multiples of 4): mean * max(net, 1e-3),
+        the network run on the tensor-core kernels."""
         mean = observed.double().mean().float().clamp_min(epsilon)
-        out = self.forward(observed / mean, sigma)[0]
+        out = self.forward(observed / mean, sigma, tensor_cores=True)[0]
         return (out.clamp_min(1e-3) * mean).contiguous()
 
     # -- weights file: magic, version, count, then little-endian f32 master parameters ---------
@@ -267,6 +310,7 @@ class WarmStartNet:
         self.master.copy_(self.torch.from_numpy(host.copy()).to(self.device))
         self.p16.copy_(self.master.to(self.torch.bfloat16))
         self._flipped = None
+        self._packed = None
 
 
 # ---------------------------------------------------------------------------------------------

@@ -205,9 +205,12 @@ int iane_gb_rl_batch_destroy(iane_gb_rl_batch* batch);
 
 /*
  * Learned warm start: kernels of a small 3-D encoder-decoder CNN (no counterpart in the
- * reference). Volumes are planar [channel][z][y][x] device arrays, activations and weights
- * BF16 (uint16_t bit patterns), accumulation FP32. Weights are [co][ci][27] with tap
- * t = tx + 3 ty + 9 tz reading x(v + (tx-1, ty-1, tz-1)) (cross-correlation).
+ * reference). Activations are BF16 (uint16_t bit patterns) in the C8 layout: channel octets,
+ * each voxel-major with its 8 channels contiguous -- element (c, v) of a volume of V voxels
+ * at ((c / 8) * V + v) * 8 + c % 8, ceil(C / 8) octets, voxels v = (z * h + y) * w + x.
+ * FP32 outputs, residuals and targets are planar [c][v]. Weights are BF16 [co][ci][27]
+ * with tap t = tx + 3 ty + 9 tz reading x(v + (tx-1, ty-1, tz-1)) (cross-correlation);
+ * accumulation is FP32.
  */
 /* y = act(bias + conv(concat(x0[c0], x1[c1]), weights) (+ residual, co == 1)), zero padding;
  * mask (co channels, optional): y *= (mask > 0). Writes y16 (bf16) and/or y32 (f32). co <= 64. */
@@ -215,7 +218,8 @@ int iane_gb_cnn_conv3(const uint16_t* x0, int c0, const uint16_t* x1, int c1, in
 	const uint16_t* weights, const float* bias, int co, uint16_t* y16, float* y32,
 	const float* residual, int act, const uint16_t* mask, void* stream);
 /* dw[co][ci][t] += sum_v dy[co](v) x[ci](v + t - 1); db[co] += sum_v dy[co](v) (FP32,
- * deterministic split-K through `scratch`). */
+ * deterministic split-K through `scratch`). c0 a multiple of 8 when c1 > 0; x0, x1 16-byte
+ * aligned. */
 size_t iane_gb_cnn_wgrad_scratch_bytes(int c0, int c1, int d, int h, int w, int co);
 int iane_gb_cnn_conv3_wgrad(const uint16_t* x0, int c0, const uint16_t* x1, int c1, int d, int h, int w,
 	const uint16_t* dy, int co, float* dw, float* db, void* scratch, size_t scratch_bytes, void* stream);
@@ -227,9 +231,18 @@ int iane_gb_cnn_pool2_grad(const uint16_t* dy, int c, int d, int h, int w, uint1
 int iane_gb_cnn_up2(const uint16_t* x, int c, int d, int h, int w, uint16_t* y, void* stream);
 int iane_gb_cnn_up2_grad(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx,
 	const uint16_t* mask, void* stream);
-/* *loss += mean((y - target)^2) (device double); dy = 2 (y - target) / n as bf16. */
+/* *loss += mean((y - target)^2) (device double); dy = 2 (y - target) / n as bf16, a
+ * one-channel C8 tensor (slot 0 of each voxel's octet). */
 int iane_gb_cnn_mse(const float* y, const float* target, long long n, uint16_t* dy, double* loss,
 	void* stream);
+/* Tensor-core forward of conv3 (tcgen05, FP32 accumulation in TMEM) on C8 inputs with
+ * weights packed by iane_gb_cnn_tc_pack. c0 is a multiple of 16 when c1 > 0; the BF16
+ * output needs co a multiple of 8; buffers 16-byte aligned. No mask operand (forward only). */
+size_t iane_gb_cnn_tc_packed_bytes(int co, int c0, int c1);
+int iane_gb_cnn_tc_pack(const uint16_t* weights, int co, int c0, int c1, uint16_t* packed, void* stream);
+int iane_gb_cnn_conv3_tc(const uint16_t* x0, int c0, const uint16_t* x1, int c1, int d, int h, int w,
+	const uint16_t* packed, const float* bias, int co, uint16_t* y16, float* y32, const float* residual,
+	int act, void* stream);
 /* Adam step on FP32 parameters (grads scaled by grad_scale), refreshing their BF16 copy. */
 int iane_gb_cnn_adam(float* params, uint16_t* params16, const float* grads, float* m, float* v,
 	long long n, float lr, float beta1, float beta2, float eps, int step, float grad_scale,

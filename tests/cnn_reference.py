@@ -83,3 +83,19 @@ def forward(p, x, residual, round_activations=True):
     d1a = layer("d1a", torch.cat([up2(d2b), e1b], 0))
     d1b = layer("d1b", d1a)
     return layer("head", d1b, relu=False) + residual.unsqueeze(0)
+
+
+def to_c8(t: torch.Tensor) -> torch.Tensor:
+    """[C][D][H][W] -> the kernels' C8 layout [ceil(C/8)][D][H][W][8] (zero-padded)."""
+    c = t.shape[0]
+    pad = (-c) % 8
+    if pad:
+        t = torch.cat([t, torch.zeros((pad,) + tuple(t.shape[1:]), dtype=t.dtype, device=t.device)], 0)
+    o = t.shape[0] // 8
+    return t.reshape((o, 8) + tuple(t.shape[1:])).permute(0, 2, 3, 4, 1).contiguous()
+
+
+def from_c8(t: torch.Tensor, c: int) -> torch.Tensor:
+    """C8 [O][D][H][W][8] -> [c][D][H][W]."""
+    o = t.shape[0]
+    return t.permute(0, 4, 1, 2, 3).reshape((o * 8,) + tuple(t.shape[1:4]))[:c]

@@ -11,7 +11,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from cnn_reference import LAYERS, bf16_round, conv3, forward, pool2, unpack, up2
+from cnn_reference import LAYERS, bf16_round, conv3, forward, from_c8, pool2, to_c8, unpack, up2
 
 pytestmark = pytest.mark.gpu
 
@@ -29,10 +29,17 @@ def _check(rc):
 
 
 def _bf16_tensor(gen, shape, scale=1.0, device="cuda"):
+    """(float64 reference, BF16 device copy) of N(0, scale^2) values rounded to BF16."""
     import torch
 
     t = torch.randn(shape, generator=gen, dtype=torch.float64) * scale
     return bf16_round(t), t.to(torch.bfloat16).to(device)
+
+
+def _act(gen, shape, scale=1.0, device="cuda"):
+    """An activation: float64 planar reference and its BF16 C8 device copy."""
+    ref, dev = _bf16_tensor(gen, shape, scale, device)
+    return ref, to_c8(dev)
 
 
 def _p(t):
@@ -51,13 +58,13 @@ def test_conv3_forward(cuda, shape, c0, c1, co):
     import torch
 
     gen = torch.Generator().manual_seed(1 + c0 + co)
-    x0r, x0 = _bf16_tensor(gen, (c0,) + shape)
-    x1r, x1 = _bf16_tensor(gen, (max(c1, 1),) + shape)
+    x0r, x0 = _act(gen, (c0,) + shape)
+    x1r, x1 = _act(gen, (max(c1, 1),) + shape)
     wr, w = _bf16_tensor(gen, (co, c0 + c1, 27), 0.2)
     b = torch.randn(co, generator=gen, dtype=torch.float32) * 0.1
     y32 = torch.empty((co,) + shape, dtype=torch.float32, device=cuda)
-    y16 = torch.empty((co,) + shape, dtype=torch.bfloat16, device=cuda)
-    mr, m = _bf16_tensor(gen, (co,) + shape)
+    y16 = to_c8(torch.zeros((co,) + shape, dtype=torch.bfloat16, device=cuda))
+    mr, m = _act(gen, (co,) + shape)
     bd = b.to(cuda)
     _check(_lib().iane_gb_cnn_conv3(_p(x0), c0, _p(x1) if c1 else None, c1, *shape, _p(w), _p(bd), co,
                                     _p(y16), _p(y32), None, 1, _p(m), None))
@@ -68,7 +75,7 @@ def test_conv3_forward(cuda, shape, c0, c1, co):
     got = y32.cpu().double()
     assert float(((got - ref).abs() / (mag + 1e-30)).max()) < 2e-6
     # BF16 output is the rounded FP32 value
-    assert torch.equal(y16.cpu(), y32.cpu().to(torch.bfloat16))
+    assert torch.equal(from_c8(y16.cpu(), co), y32.cpu().to(torch.bfloat16))
 
 
 def test_conv3_residual_f32_output(cuda):
@@ -76,7 +83,7 @@ def test_conv3_residual_f32_output(cuda):
 
     gen = torch.Generator().manual_seed(7)
     shape = (8, 12, 20)
-    xr, x = _bf16_tensor(gen, (16,) + shape)
+    xr, x = _act(gen, (16,) + shape)
     wr, w = _bf16_tensor(gen, (1, 16, 27), 0.2)
     res = torch.randn((1,) + shape, generator=gen, dtype=torch.float32)
     b = torch.tensor([0.25], dtype=torch.float32)
@@ -97,7 +104,7 @@ def test_conv3_input_gradient_by_flipped_weights(cuda, shape, ci, co):
 
     gen = torch.Generator().manual_seed(ci * 100 + co)
     xr = torch.randn((ci,) + shape, generator=gen, dtype=torch.float64).requires_grad_(True)
-    dyr, dy = _bf16_tensor(gen, (co,) + shape)
+    dyr, dy = _act(gen, (co,) + shape)
     wr, w = _bf16_tensor(gen, (co, ci, 27), 0.2)
     (conv3(xr, wr) * dyr).sum().backward()
     ref = xr.grad
@@ -113,15 +120,15 @@ def test_conv3_input_gradient_by_flipped_weights(cuda, shape, ci, co):
     assert torch.equal(flipped.cpu(), wt.to(torch.bfloat16).reshape(-1))
 
 
-@pytest.mark.parametrize("shape,c0,c1,co", [((6, 10, 12), 16, 0, 16), ((5, 9, 17), 3, 5, 20), ((8, 8, 8), 32, 16, 48),
+@pytest.mark.parametrize("shape,c0,c1,co", [((6, 10, 12), 16, 0, 16), ((5, 9, 17), 8, 5, 20), ((8, 8, 8), 32, 16, 48),
                                              ((16, 16, 16), 2, 0, 16), ((7, 3, 11), 16, 0, 1)])
 def test_conv3_weight_gradient(cuda, shape, c0, c1, co):
     import torch
 
     gen = torch.Generator().manual_seed(3 * c0 + co)
-    x0r, x0 = _bf16_tensor(gen, (c0,) + shape)
-    x1r, x1 = _bf16_tensor(gen, (max(c1, 1),) + shape)
-    dyr, dy = _bf16_tensor(gen, (co,) + shape)
+    x0r, x0 = _act(gen, (c0,) + shape)
+    x1r, x1 = _act(gen, (max(c1, 1),) + shape)
+    dyr, dy = _act(gen, (co,) + shape)
     inp = torch.cat([x0r, x1r[:c1]], 0) if c1 else x0r
     wr = torch.zeros((co, c0 + c1, 27), dtype=torch.float64, requires_grad=True)
     br = torch.zeros(co, dtype=torch.float64, requires_grad=True)
@@ -155,8 +162,8 @@ def test_conv3_wgrad_scratch_too_small_is_a_length_error(cuda):
 
     from iane_gb300 import abi
 
-    x = torch.zeros((4, 8, 8, 8), dtype=torch.bfloat16, device=cuda)
-    dy = torch.zeros((4, 8, 8, 8), dtype=torch.bfloat16, device=cuda)
+    x = torch.zeros((1, 8, 8, 8, 8), dtype=torch.bfloat16, device=cuda)
+    dy = torch.zeros((1, 8, 8, 8, 8), dtype=torch.bfloat16, device=cuda)
     dw = torch.zeros(4 * 4 * 27, dtype=torch.float32, device=cuda)
     scratch = torch.empty(16, dtype=torch.uint8, device=cuda)
     rc = _lib().iane_gb_cnn_conv3_wgrad(_p(x), 4, None, 0, 8, 8, 8, _p(dy), 4, _p(dw), None, _p(scratch), 16, None)
@@ -169,34 +176,34 @@ def test_pool_and_upsample(cuda):
     gen = torch.Generator().manual_seed(11)
     c, shape = 5, (6, 8, 10)
     half = tuple(s // 2 for s in shape)
-    xr, x = _bf16_tensor(gen, (c,) + shape)
-    y = torch.empty((c,) + half, dtype=torch.bfloat16, device=cuda)
+    xr, x = _act(gen, (c,) + shape)
+    y = to_c8(torch.zeros((c,) + half, dtype=torch.bfloat16, device=cuda))
     _check(_lib().iane_gb_cnn_pool2(_p(x), c, *shape, _p(y), None))
     torch.cuda.synchronize()
     # 8 BF16 values summed in FP32 and scaled by 1/8: the FP32 sum is exact to 2^-24 relative
-    assert torch.allclose(y.cpu().double(), bf16_round(pool2(xr)), rtol=2 ** -8, atol=0)
+    assert torch.allclose(from_c8(y.cpu(), c).double(), bf16_round(pool2(xr)), rtol=2 ** -8, atol=0)
 
-    dyr, dy = _bf16_tensor(gen, (c,) + half)
-    mr, m = _bf16_tensor(gen, (c,) + shape)
+    dyr, dy = _act(gen, (c,) + half)
+    mr, m = _act(gen, (c,) + shape)
     for accumulate in (0, 1):
-        pr, prev = _bf16_tensor(gen, (c,) + shape)
+        pr, prev = _act(gen, (c,) + shape)
         dx = prev.clone()
         _check(_lib().iane_gb_cnn_pool2_grad(_p(dy), c, *shape, _p(dx), _p(m), accumulate, None))
         torch.cuda.synchronize()
         ref = (up2(dyr) / 8 + (pr if accumulate else 0)) * (mr > 0)
-        assert torch.allclose(dx.cpu().double(), bf16_round(ref), rtol=2 ** -8, atol=0)
+        assert torch.allclose(from_c8(dx.cpu(), c).double(), bf16_round(ref), rtol=2 ** -8, atol=0)
 
-    u = torch.empty((c,) + tuple(2 * s for s in shape), dtype=torch.bfloat16, device=cuda)
+    u = to_c8(torch.zeros((c,) + tuple(2 * s for s in shape), dtype=torch.bfloat16, device=cuda))
     _check(_lib().iane_gb_cnn_up2(_p(x), c, *shape, _p(u), None))
     torch.cuda.synchronize()
-    assert torch.equal(u.cpu().double(), up2(xr))
+    assert torch.equal(from_c8(u.cpu(), c).double(), up2(xr))
 
-    gr, g = _bf16_tensor(gen, (c,) + tuple(2 * s for s in shape))
-    dx = torch.empty((c,) + shape, dtype=torch.bfloat16, device=cuda)
+    gr, g = _act(gen, (c,) + tuple(2 * s for s in shape))
+    dx = to_c8(torch.zeros((c,) + shape, dtype=torch.bfloat16, device=cuda))
     _check(_lib().iane_gb_cnn_up2_grad(_p(g), c, *shape, _p(dx), _p(m), None))
     torch.cuda.synchronize()
     ref = (gr.reshape(c, shape[0], 2, shape[1], 2, shape[2], 2).sum((2, 4, 6))) * (mr > 0)
-    assert torch.allclose(dx.cpu().double(), bf16_round(ref), rtol=2 ** -8, atol=0)
+    assert torch.allclose(from_c8(dx.cpu(), c).double(), bf16_round(ref), rtol=2 ** -8, atol=0)
 
 
 def test_mse_and_adam(cuda):
@@ -206,14 +213,15 @@ def test_mse_and_adam(cuda):
     n = 100003
     y = torch.randn(n, generator=gen, dtype=torch.float32)
     t = torch.randn(n, generator=gen, dtype=torch.float32)
-    dy = torch.empty(n, dtype=torch.bfloat16, device=cuda)
+    dy = torch.zeros(8 * n, dtype=torch.bfloat16, device=cuda)  # one channel, C8
     loss = torch.full((1,), 0.5, dtype=torch.float64, device=cuda)
     yd, td = y.to(cuda), t.to(cuda)
     _check(_lib().iane_gb_cnn_mse(_p(yd), _p(td), n, _p(dy), _p(loss), None))
     torch.cuda.synchronize()
     e = (y - t).double()
     assert abs(float(loss.item()) - 0.5 - float((e * e).mean())) < 1e-12
-    assert torch.equal(dy.cpu(), (2.0 * (y - t) / n).to(torch.bfloat16))
+    assert torch.equal(dy.cpu()[::8], (2.0 * (y - t) / n).to(torch.bfloat16))
+    assert not bool(dy.cpu().reshape(n, 8)[:, 1:].any())
 
     p = torch.randn(n, generator=gen, dtype=torch.float32)
     g = torch.randn(n, generator=gen, dtype=torch.float32)
@@ -234,6 +242,81 @@ def test_mse_and_adam(cuda):
     assert float((dv.cpu().double() - v1).abs().max()) < 1e-6
     assert float((dp.cpu().double() - p1).abs().max()) < 1e-6
     assert torch.equal(dp16.cpu(), dp.cpu().to(torch.bfloat16))
+
+
+@pytest.mark.parametrize("shape,c0,c1,co", [((6, 10, 12), 16, 0, 16), ((5, 9, 30), 2, 0, 16), ((4, 8, 16), 64, 32, 32),
+                                             ((3, 5, 7), 32, 0, 64), ((8, 12, 29), 32, 16, 16), ((9, 17, 15), 16, 0, 32)])
+def test_conv3_tensor_core_forward(cuda, shape, c0, c1, co):
+    """tcgen05 forward against float64 (BF16 products are exact in FP32; the error is the
+    FP32 accumulation) and against the SIMT kernel."""
+    import torch
+
+    gen = torch.Generator().manual_seed(17 + c0 + co + shape[2])
+    x0r, x0 = _act(gen, (c0,) + shape)
+    x1r, x1 = _act(gen, (max(c1, 1),) + shape)
+    wr, w = _bf16_tensor(gen, (co, c0 + c1, 27), 0.2)
+    b = (torch.randn(co, generator=gen, dtype=torch.float32) * 0.1).to(cuda)
+    packed = torch.empty(int(_lib().iane_gb_cnn_tc_packed_bytes(co, c0, c1)) // 2, dtype=torch.bfloat16, device=cuda)
+    _check(_lib().iane_gb_cnn_tc_pack(_p(w), co, c0, c1, _p(packed), None))
+    y16 = to_c8(torch.zeros((co,) + shape, dtype=torch.bfloat16, device=cuda))
+    y32 = torch.zeros((co,) + shape, dtype=torch.float32, device=cuda)
+    _check(_lib().iane_gb_cnn_conv3_tc(_p(x0), c0, _p(x1) if c1 else None, c1, *shape, _p(packed), _p(b), co,
+                                       _p(y16), _p(y32), None, 1, None))
+    s16 = to_c8(torch.zeros((co,) + shape, dtype=torch.bfloat16, device=cuda))
+    s32 = torch.zeros((co,) + shape, dtype=torch.float32, device=cuda)
+    _check(_lib().iane_gb_cnn_conv3(_p(x0), c0, _p(x1) if c1 else None, c1, *shape, _p(w), _p(b), co, _p(s16),
+                                    _p(s32), None, 1, None, None))
+    torch.cuda.synchronize()
+    from iane_gb300 import device_status
+
+    device_status()
+    inp = torch.cat([x0r, x1r[:c1]], 0) if c1 else x0r
+    ref = torch.relu(conv3(inp, wr, b.cpu().double()))
+    mag = conv3(inp.abs(), wr.abs()) + b.cpu().double().abs().reshape(-1, 1, 1, 1)
+    got = y32.cpu().double()
+    assert float(((got - ref).abs() / mag).max()) < 1e-5
+    assert float(((got - s32.cpu().double()).abs() / mag).max()) < 1e-5
+    assert torch.equal(from_c8(y16.cpu(), co), y32.cpu().to(torch.bfloat16))
+
+
+def test_conv3_tensor_core_head_with_residual(cuda):
+    import torch
+
+    gen = torch.Generator().manual_seed(23)
+    shape = (7, 13, 33)
+    xr, x = _act(gen, (16,) + shape)
+    wr, w = _bf16_tensor(gen, (1, 16, 27), 0.2)
+    res = torch.randn((1,) + shape, generator=gen, dtype=torch.float32).to(cuda)
+    b = torch.tensor([0.25], dtype=torch.float32, device=cuda)
+    packed = torch.empty(int(_lib().iane_gb_cnn_tc_packed_bytes(1, 16, 0)) // 2, dtype=torch.bfloat16, device=cuda)
+    _check(_lib().iane_gb_cnn_tc_pack(_p(w), 1, 16, 0, _p(packed), None))
+    y = torch.zeros((1,) + shape, dtype=torch.float32, device=cuda)
+    _check(_lib().iane_gb_cnn_conv3_tc(_p(x), 16, None, 0, *shape, _p(packed), _p(b), 1, None, _p(y), _p(res), 0,
+                                       None))
+    torch.cuda.synchronize()
+    ref = conv3(xr, wr, b.cpu().double()) + res.cpu().double()
+    mag = conv3(xr.abs(), wr.abs()) + 0.25 + res.cpu().double().abs()
+    assert float(((y.cpu().double() - ref).abs() / mag).max()) < 1e-5
+
+
+def test_network_tensor_core_forward_matches_simt(cuda):
+    import torch
+
+    from iane_gb300.learned import WarmStartNet
+
+    net = WarmStartNet(cuda, seed=6)
+    gen = torch.Generator().manual_seed(4)
+    w0, b0 = net.offsets["head"]
+    net.master[w0:b0] = (torch.randn(b0 - w0, generator=gen) * 0.3).to(cuda)
+    net.p16.copy_(net.master.to(torch.bfloat16))
+    obs = (torch.rand((16, 36, 44), generator=gen, dtype=torch.float32) * 2.0).to(cuda)
+    a = net.forward(obs, 1.5).clone()
+    b = net.forward(obs, 1.5, tensor_cores=True).clone()
+    torch.cuda.synchronize()
+    # the paths sum in different FP32 orders (each layer agrees to 1e-5 of its magnitude, see
+    # above), which flips the BF16 rounding (2^-8 relative) of some stored activations; over
+    # eleven layers that leaves a few 1e-3 of difference in the output
+    assert _rel_l2(b.cpu(), a.cpu()) < 1e-2
 
 
 def test_network_forward_and_gradients_match_float64(cuda):
