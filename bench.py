@@ -315,6 +315,17 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30):
             "prepare_s": prepare_s}
 
 
+def measure_learned_leg(dev):
+    """Learned warm start: the shipped network's start + BF16 tensor-core RL against plain FP32
+    RL from the flat start on the 256x256x64 ellipsoid volume (200 ellipsoids), isotropic
+    Gaussian PSF sigma 2 (11^3), Poisson peak 1000; reference = 200 FP32 iterations. Stopping
+    rules, iteration counts, wall times (CUDA events) and errors as iane_gb300.learned.evaluate
+    reports them."""
+    from iane_gb300.learned import evaluate, load_default
+
+    return evaluate(load_default(dev), device=dev)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -412,6 +423,7 @@ def main():
     hbm_legs = measure_hbm_legs(dev, stream)
     bf16_leg = measure_bf16_leg(dev, stream)
     batch_leg = measure_batch_leg(dev, stream)
+    learned_leg = measure_learned_leg(dev)
 
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
@@ -470,6 +482,7 @@ def main():
             "hbm_legs": hbm_legs,
             "bf16_tensor_leg": bf16_leg,
             "batch_leg": batch_leg,
+            "learned_warm_start_leg": learned_leg,
         }
         print(json.dumps(line), flush=True)
     rl.close()

@@ -267,82 +267,117 @@ __global__ void flip_kernel(const uint16_t* w, int co, int ci, uint16_t* wt)
 	}
 }
 
-// Average pooling 2x2x2 (input d, h, w even) and its gradient (optionally masked by the
-// pooled layer's input activations). C8 tensors are indexed flat: (octet, voxel, lane).
-__global__ void pool2_kernel(const uint16_t* x, int c, int d, int h, int w, uint16_t* y)
+// Average pooling 2x2x2 (input d, h, w even), nearest upsampling x2 and their gradients on C8
+// tensors: one thread per (voxel, octet), 16-byte vector loads and stores. Grid: x over
+// blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, (octet, z) folded into blockIdx.z
+// (grid-strided); the extents are those of the tensor the thread writes.
+__device__ __forceinline__ void unpack8(const uint4 q, float (&f)[8])
+{
+	const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		f[2 * k] = __uint_as_float(w[k] << 16);
+		f[2 * k + 1] = __uint_as_float(w[k] & 0xFFFF0000u);
+	}
+}
+
+__device__ __forceinline__ uint4 pack8(const float (&f)[8])
+{
+	uint4 q;
+	q.x = static_cast<uint32_t>(to_bf(f[0])) | (static_cast<uint32_t>(to_bf(f[1])) << 16);
+	q.y = static_cast<uint32_t>(to_bf(f[2])) | (static_cast<uint32_t>(to_bf(f[3])) << 16);
+	q.z = static_cast<uint32_t>(to_bf(f[4])) | (static_cast<uint32_t>(to_bf(f[5])) << 16);
+	q.w = static_cast<uint32_t>(to_bf(f[6])) | (static_cast<uint32_t>(to_bf(f[7])) << 16);
+	return q;
+}
+
+// out-extents (od, oh, ow), octets; x = thread index, y = blockIdx.y, (oct, z) from blockIdx.z
+#define IANE_GB_C8_LOOP(od, oh, ow, octets)                                                                    \
+	const int x = blockIdx.x * blockDim.x + threadIdx.x;                                                       \
+	const int y = blockIdx.y;                                                                                  \
+	if (x >= (ow) || y >= (oh)) return;                                                                        \
+	for (int zo = blockIdx.z; zo < (od) * (octets); zo += gridDim.z)
+
+__global__ void pool2_kernel(const uint4* x_, int octets, int d, int h, int w, uint4* y_)
 {
 	const int od = d / 2, oh = h / 2, ow = w / 2;
-	const long long ovol = static_cast<long long>(od) * oh * ow, ivol = static_cast<long long>(d) * h * w;
-	const long long n = static_cast<long long>((c + 7) / 8) * ovol * 8;
-	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int lane = static_cast<int>(i & 7);
-		const long long ov = (i >> 3) % ovol, oct = (i >> 3) / ovol;
-		const int ox = static_cast<int>(ov % ow), oy = static_cast<int>((ov / ow) % oh), oz = static_cast<int>(ov / (static_cast<long long>(ow) * oh));
-		const uint16_t* src = x + oct * ivol * 8 + lane;
-		float s = 0.0f;
+	const long long ivol = static_cast<long long>(d) * h * w, ovol = static_cast<long long>(od) * oh * ow;
+	IANE_GB_C8_LOOP(od, oh, ow, octets)
+	{
+		const int z = zo % od, oct = zo / od;
+		const uint4* src = x_ + oct * ivol;
+		float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 		for (int k = 0; k < 8; ++k) {
-			const long long v = (2 * oz + (k >> 2)) * static_cast<long long>(h) * w + (2 * oy + ((k >> 1) & 1)) * w + 2 * ox + (k & 1);
-			s += bf(src[v * 8]);
+			float f[8];
+			unpack8(src[(2LL * z + (k >> 2)) * h * w + static_cast<long long>(2 * y + ((k >> 1) & 1)) * w + 2 * x + (k & 1)], f);
+#pragma unroll
+			for (int c = 0; c < 8; ++c) s[c] += f[c];
 		}
-		y[i] = to_bf(0.125f * s);
+#pragma unroll
+		for (int c = 0; c < 8; ++c) s[c] *= 0.125f;
+		y_[oct * ovol + (static_cast<long long>(z) * oh + y) * ow + x] = pack8(s);
 	}
 }
 
-__global__ void pool2_grad_kernel(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx, const uint16_t* mask,
+__global__ void pool2_grad_kernel(const uint4* dy_, int octets, int d, int h, int w, uint4* dx_, const uint4* mask_,
 	int accumulate)
 {
-	const long long ivol = static_cast<long long>(d) * h * w;
-	const long long ovol = ivol / 8;
-	const long long n = static_cast<long long>((c + 7) / 8) * ivol * 8;
-	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int lane = static_cast<int>(i & 7);
-		const long long v = (i >> 3) % ivol, oct = (i >> 3) / ivol;
-		const int xx = static_cast<int>(v % w), yy = static_cast<int>((v / w) % h), zz = static_cast<int>(v / (static_cast<long long>(w) * h));
-		const long long o = (static_cast<long long>(zz / 2) * (h / 2) + yy / 2) * (w / 2) + xx / 2;
-		float g = 0.125f * bf(dy[((oct * ovol + o) << 3) + lane]);
-		if (accumulate) g += bf(dx[i]);
-		if (mask && !(bf(mask[i]) > 0.0f)) g = 0.0f;
-		dx[i] = to_bf(g);
+	const long long ivol = static_cast<long long>(d) * h * w, ovol = ivol / 8;
+	IANE_GB_C8_LOOP(d, h, w, octets)
+	{
+		const int z = zo % d, oct = zo / d;
+		const long long at = oct * ivol + (static_cast<long long>(z) * h + y) * w + x;
+		float g[8], m[8], prev[8];
+		unpack8(dy_[oct * ovol + (static_cast<long long>(z / 2) * (h / 2) + y / 2) * (w / 2) + x / 2], g);
+		if (accumulate) unpack8(dx_[at], prev);
+		if (mask_) unpack8(mask_[at], m);
+#pragma unroll
+		for (int c = 0; c < 8; ++c) {
+			g[c] *= 0.125f;
+			if (accumulate) g[c] += prev[c];
+			if (mask_ && !(m[c] > 0.0f)) g[c] = 0.0f;
+		}
+		dx_[at] = pack8(g);
 	}
 }
 
-// Nearest upsampling x2 (d, h, w: input extents) and its gradient (sum of the 8 children).
-__global__ void up2_kernel(const uint16_t* x, int c, int d, int h, int w, uint16_t* y)
+__global__ void up2_kernel(const uint4* x_, int octets, int d, int h, int w, uint4* y_)
 {
 	const int od = 2 * d, oh = 2 * h, ow = 2 * w;
-	const long long ovol = static_cast<long long>(od) * oh * ow, ivol = static_cast<long long>(d) * h * w;
-	const long long n = static_cast<long long>((c + 7) / 8) * ovol * 8;
-	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int lane = static_cast<int>(i & 7);
-		const long long ov = (i >> 3) % ovol, oct = (i >> 3) / ovol;
-		const int ox = static_cast<int>(ov % ow), oy = static_cast<int>((ov / ow) % oh), oz = static_cast<int>(ov / (static_cast<long long>(ow) * oh));
-		const long long v = (static_cast<long long>(oz / 2) * h + oy / 2) * w + ox / 2;
-		y[i] = x[((oct * ivol + v) << 3) + lane];
+	const long long ivol = static_cast<long long>(d) * h * w, ovol = 8 * ivol;
+	IANE_GB_C8_LOOP(od, oh, ow, octets)
+	{
+		const int z = zo % od, oct = zo / od;
+		y_[oct * ovol + (static_cast<long long>(z) * oh + y) * ow + x] =
+			x_[oct * ivol + (static_cast<long long>(z / 2) * h + y / 2) * w + x / 2];
 	}
 }
 
-__global__ void up2_grad_kernel(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx, const uint16_t* mask)
+__global__ void up2_grad_kernel(const uint4* dy_, int octets, int d, int h, int w, uint4* dx_, const uint4* mask_)
 {
 	const long long ivol = static_cast<long long>(d) * h * w, ovol = 8 * ivol;
-	const long long n = static_cast<long long>((c + 7) / 8) * ivol * 8;
-	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int lane = static_cast<int>(i & 7);
-		const long long v = (i >> 3) % ivol, oct = (i >> 3) / ivol;
-		const int xx = static_cast<int>(v % w), yy = static_cast<int>((v / w) % h), zz = static_cast<int>(v / (static_cast<long long>(w) * h));
-		const uint16_t* src = dy + oct * ovol * 8 + lane;
-		float s = 0.0f;
+	IANE_GB_C8_LOOP(d, h, w, octets)
+	{
+		const int z = zo % d, oct = zo / d;
+		const uint4* src = dy_ + oct * ovol;
+		float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 		for (int k = 0; k < 8; ++k) {
-			const long long o = (2 * zz + (k >> 2)) * 4LL * h * w + (2 * yy + ((k >> 1) & 1)) * 2LL * w + 2 * xx + (k & 1);
-			s += bf(src[o * 8]);
+			float f[8];
+			unpack8(src[(2LL * z + (k >> 2)) * 4 * h * w + static_cast<long long>(2 * y + ((k >> 1) & 1)) * 2 * w + 2 * x + (k & 1)], f);
+#pragma unroll
+			for (int c = 0; c < 8; ++c) s[c] += f[c];
 		}
-		if (mask && !(bf(mask[i]) > 0.0f)) s = 0.0f;
-		dx[i] = to_bf(s);
+		const long long at = oct * ivol + (static_cast<long long>(z) * h + y) * w + x;
+		if (mask_) {
+			float m[8];
+			unpack8(mask_[at], m);
+#pragma unroll
+			for (int c = 0; c < 8; ++c) if (!(m[c] > 0.0f)) s[c] = 0.0f;
+		}
+		dx_[at] = pack8(s);
 	}
 }
+#undef IANE_GB_C8_LOOP
 
 // loss = sum (y - t)^2 / n (FP64 accumulation per CTA, atomically added), dy = 2 (y - t) / n
 // (a one-channel C8 tensor: slot 0 of each voxel's octet).
@@ -391,6 +426,16 @@ long long wgrad_chunks(int c0, int c1, int d, int h, int w, int co)
 	const int octets = (c0 + 7) / 8 + (c1 + 7) / 8;
 	long long chunks = (4LL * device_sm_count()) / (co_tiles * octets);
 	return chunks < 1 ? 1 : (chunks > bricks ? bricks : chunks);
+}
+
+bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
+
+// Grid of the C8 elementwise kernels: 128 threads along x, one block row per y, (z, octet)
+// pairs along grid z (capped; the kernels stride over the rest).
+dim3 c8_grid(int ow, int oh, long long zo)
+{
+	return dim3(static_cast<unsigned>((ow + 127) / 128), static_cast<unsigned>(oh),
+		static_cast<unsigned>(zo < 65535 ? zo : 65535));
 }
 
 int grid1(long long n)
@@ -493,9 +538,12 @@ int iane_gb_cnn_flip(const uint16_t* weights, int co, int ci, uint16_t* flipped,
 
 int iane_gb_cnn_pool2(const uint16_t* x, int c, int d, int h, int w, uint16_t* y, void* stream)
 {
-	if (!x || !y || c < 1 || d % 2 || h % 2 || w % 2 || d < 2) return fail(IANE_GB_INVALID_ARGUMENT, "cnn_pool2: even extents");
-	pool2_kernel<<<grid1(static_cast<long long>(c) * d * h * w / 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, c,
-		d, h, w, y);
+	if (!x || !y || c < 1 || d % 2 || h % 2 || w % 2 || d < 2 || !aligned16(x) || !aligned16(y) || h / 2 > 65535) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_pool2: even extents, 16-byte aligned C8 tensors");
+	}
+	const int oct = (c + 7) / 8;
+	pool2_kernel<<<c8_grid(w / 2, h / 2, d / 2 * oct), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+		reinterpret_cast<const uint4*>(x), oct, d, h, w, reinterpret_cast<uint4*>(y));
 	IANE_GB_CUDA(cudaGetLastError(), "cnn_pool2: launch");
 	return IANE_GB_OK;
 }
@@ -503,17 +551,25 @@ int iane_gb_cnn_pool2(const uint16_t* x, int c, int d, int h, int w, uint16_t* y
 int iane_gb_cnn_pool2_grad(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx, const uint16_t* mask,
 	int accumulate, void* stream)
 {
-	if (!dy || !dx || c < 1 || d % 2 || h % 2 || w % 2) return fail(IANE_GB_INVALID_ARGUMENT, "cnn_pool2_grad: bad arguments");
-	pool2_grad_kernel<<<grid1(static_cast<long long>(c) * d * h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(dy,
-		c, d, h, w, dx, mask, accumulate);
+	if (!dy || !dx || c < 1 || d % 2 || h % 2 || w % 2 || !aligned16(dy) || !aligned16(dx) || !aligned16(mask) || h > 65535) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_pool2_grad: even extents, 16-byte aligned C8 tensors");
+	}
+	const int oct = (c + 7) / 8;
+	pool2_grad_kernel<<<c8_grid(w, h, d * oct), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+		reinterpret_cast<const uint4*>(dy), oct, d, h, w, reinterpret_cast<uint4*>(dx), reinterpret_cast<const uint4*>(mask),
+		accumulate);
 	IANE_GB_CUDA(cudaGetLastError(), "cnn_pool2_grad: launch");
 	return IANE_GB_OK;
 }
 
 int iane_gb_cnn_up2(const uint16_t* x, int c, int d, int h, int w, uint16_t* y, void* stream)
 {
-	if (!x || !y || c < 1 || d < 1 || h < 1 || w < 1) return fail(IANE_GB_INVALID_ARGUMENT, "cnn_up2: bad arguments");
-	up2_kernel<<<grid1(8LL * c * d * h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, c, d, h, w, y);
+	if (!x || !y || c < 1 || d < 1 || h < 1 || w < 1 || !aligned16(x) || !aligned16(y) || 2 * h > 65535) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_up2: bad arguments");
+	}
+	const int oct = (c + 7) / 8;
+	up2_kernel<<<c8_grid(2 * w, 2 * h, 2 * d * oct), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+		reinterpret_cast<const uint4*>(x), oct, d, h, w, reinterpret_cast<uint4*>(y));
 	IANE_GB_CUDA(cudaGetLastError(), "cnn_up2: launch");
 	return IANE_GB_OK;
 }
@@ -521,9 +577,13 @@ int iane_gb_cnn_up2(const uint16_t* x, int c, int d, int h, int w, uint16_t* y, 
 int iane_gb_cnn_up2_grad(const uint16_t* dy, int c, int d, int h, int w, uint16_t* dx, const uint16_t* mask,
 	void* stream)
 {
-	if (!dy || !dx || c < 1) return fail(IANE_GB_INVALID_ARGUMENT, "cnn_up2_grad: bad arguments");
-	up2_grad_kernel<<<grid1(static_cast<long long>(c) * d * h * w), 256, 0, static_cast<cudaStream_t>(stream)>>>(dy, c,
-		d, h, w, dx, mask);
+	if (!dy || !dx || c < 1 || d < 1 || h < 1 || w < 1 || !aligned16(dy) || !aligned16(dx) || !aligned16(mask) ||
+	    h > 65535) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_up2_grad: bad arguments");
+	}
+	const int oct = (c + 7) / 8;
+	up2_grad_kernel<<<c8_grid(w, h, d * oct), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+		reinterpret_cast<const uint4*>(dy), oct, d, h, w, reinterpret_cast<uint4*>(dx), reinterpret_cast<const uint4*>(mask));
 	IANE_GB_CUDA(cudaGetLastError(), "cnn_up2_grad: launch");
 	return IANE_GB_OK;
 }

@@ -12,14 +12,20 @@
 // has its own accumulator and the epilogue forms out[r] = D_0[r - 1] + D_1[r] + D_2[r + 1]
 // by lane shuffles, so rows r % 16 in 1..14 are outputs (14 columns per block) and the A
 // operand of every tap is the same shared-memory tile at a row offset -- a descriptor start
-// address, no data movement.
+// address, no data movement. Because the three tx accumulators share that A operand, the
+// weights of the three x taps are stacked along N: one MMA of N = 3 x (16, 32 or 64) per
+// (ty, tz) fills D_0 | D_1 | D_2 side by side in TMEM. (Three separate N-wide MMAs would read
+// the 4 KB A tile from shared memory three times; at N = 16 those operand reads, not the
+// math, bound the kernel.)
 //
 // Input tile: one 5-D TMA box of the C8 activation tensor, dims (8 channels, x, y, z,
 // octet), box (8, 16, 10, BZ + 2, 2) -> shared memory [octet][z][y][x][8 channels]: every 8
 // consecutive voxels of an octet are one 128-byte K-major core matrix (LBO = the octet
 // stride, SBO = 128 bytes). Out-of-range voxels and octets arrive as zeros (the padding).
-// Weights: packed per 16-channel step as [tap][8-channel half][n][8] (a K-major N x 16
-// operand per tap), one 1-D bulk copy per step. Two stages; one thread issues TMA and MMAs,
+// BZ = 2 planes per block; TMEM holds 3 x BZ x N columns (128, 256 or 512 for N = 16, 32,
+// 64), which also sets how many CTAs share an SM (4, 2, 1).
+// Weights: packed per 16-channel step as [ty, tz][8-channel half][tx][n][8] (a K-major
+// 3N x 16 operand per (ty, tz)), one 1-D bulk copy per step. Two stages; one thread issues TMA and MMAs,
 // four warps run the epilogue (bias, ReLU, BF16 C8 store or FP32 planar store + residual).
 #include "common.cuh"
 #include "tc.cuh"
@@ -32,7 +38,7 @@ namespace {
 constexpr int TX = 16, TY = 8;           // voxels per M tile (x, y)
 constexpr int OUT_X = 14;                // output columns per block
 constexpr int HY = TY + 2;               // halo rows
-constexpr int STAGES = 2;
+constexpr int MAX_STAGES = 2;
 
 __device__ __forceinline__ uint16_t to_bf16(float f)
 {
@@ -47,12 +53,12 @@ __host__ __device__ constexpr int tmem_cols(int n, int bz)
 {
 	return 3 * bz * n <= 32 ? 32 : (3 * bz * n <= 64 ? 64 : (3 * bz * n <= 128 ? 128 : (3 * bz * n <= 256 ? 256 : 512)));
 }
-__host__ __device__ constexpr size_t smem_total(int n, int bz) { return STAGES * stage_bytes(n, bz) + 8 * 8; }
+__host__ __device__ constexpr size_t smem_total(int n, int bz, int stages) { return stages * stage_bytes(n, bz) + 8 * 8; }
 
 struct TcConvArgs {
 	int d, h, w;
 	int steps0, steps;        // 16-channel K steps from x0, and in all
-	const uint16_t* packed;   // [steps][27][2][N][8]
+	const uint16_t* packed;   // [steps][9 (ty, tz)][2][3 tx][N][8]
 	const float* bias;        // [co] or null
 	int co;
 	uint16_t* y16;            // C8 output or null
@@ -60,6 +66,7 @@ struct TcConvArgs {
 	const float* residual;    // planar FP32, added before the activation, or null
 	int act;
 	int tiles_x, tiles_y;
+	int stages;               // 1 (single K step) or 2
 	int* status;
 };
 
@@ -72,11 +79,12 @@ __global__ void __launch_bounds__(128) cnn_tc_conv_kernel(const __grid_constant_
 	constexpr int AB = a_bytes(BZ);
 	constexpr uint32_t OCTET = (BZ + 2) * HY * TX * 16;  // LBO of the A operand
 	constexpr int COLS = tmem_cols(N, BZ);
-	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * SB);
+	const int S = a.stages;
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * SB);
 	uint64_t* full = bars;
-	uint64_t* empty = bars + STAGES;
-	uint64_t* done = bars + 2 * STAGES;
-	uint32_t& tmem_base_s = *reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+	uint64_t* empty = bars + S;
+	uint64_t* done = bars + 2 * S;
+	uint32_t& tmem_base_s = *reinterpret_cast<uint32_t*>(bars + 2 * S + 1);
 
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const int tx_i = blockIdx.x % a.tiles_x, ty_i = blockIdx.x / a.tiles_x;
@@ -84,7 +92,7 @@ __global__ void __launch_bounds__(128) cnn_tc_conv_kernel(const __grid_constant_
 
 	if (warp == 0) tc::tmem_alloc(&tmem_base_s, COLS);
 	if (tid == 0) {
-		for (int s = 0; s < 2 * STAGES + 1; ++s) mbar_init(&bars[s], 1);
+		for (int s = 0; s < 2 * S + 1; ++s) mbar_init(&bars[s], 1);
 		fence_barrier_init();
 	}
 	tc::fence_before_sync();
@@ -93,22 +101,22 @@ __global__ void __launch_bounds__(128) cnn_tc_conv_kernel(const __grid_constant_
 	const uint32_t tmem = tmem_base_s;
 
 	if (tid == 0) {
-		const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+		const uint32_t idesc = tc::idesc_bf16_f32(128, 3 * N);
 		auto load = [&](int p) {
-			unsigned char* st = smem + (p % STAGES) * SB;
-			mbar_arrive_expect_tx(&full[p % STAGES], static_cast<uint32_t>(SB));
+			unsigned char* st = smem + (p % S) * SB;
+			mbar_arrive_expect_tx(&full[p % S], static_cast<uint32_t>(SB));
 			if (p < a.steps0) {
-				tma_load_5d(st, &map0, 0, x0 - 1, y0 - 1, z0 - 1, 2 * p, &full[p % STAGES]);
+				tma_load_5d(st, &map0, 0, x0 - 1, y0 - 1, z0 - 1, 2 * p, &full[p % S]);
 			} else {
-				tma_load_5d(st, &map1, 0, x0 - 1, y0 - 1, z0 - 1, 2 * (p - a.steps0), &full[p % STAGES]);
+				tma_load_5d(st, &map1, 0, x0 - 1, y0 - 1, z0 - 1, 2 * (p - a.steps0), &full[p % S]);
 			}
-			tc::bulk_load(st + AB, a.packed + static_cast<size_t>(p) * (b_bytes(N) / 2), b_bytes(N), &full[p % STAGES]);
+			tc::bulk_load(st + AB, a.packed + static_cast<size_t>(p) * (b_bytes(N) / 2), b_bytes(N), &full[p % S]);
 		};
 		bool ok = true;
-		for (int p = 0; p < STAGES && p < a.steps; ++p) load(p);
+		for (int p = 0; p < S && p < a.steps; ++p) load(p);
 		for (int p = 0; p < a.steps; ++p) {
-			const int s = p % STAGES;
-			if (ok && !mbar_wait_bounded(&full[s], (p / STAGES) & 1)) {
+			const int s = p % S;
+			if (ok && !mbar_wait_bounded(&full[s], (p / S) & 1)) {
 				ok = false;
 				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
@@ -124,24 +132,23 @@ __global__ void __launch_bounds__(128) cnn_tc_conv_kernel(const __grid_constant_
 						const uint32_t a_start = a_base + static_cast<uint32_t>(((zb + tz) * HY + ty) * TX * 16);
 						const uint64_t ad = tc::smem_desc(a_start, OCTET, 128);
 						const bool acc = p > 0 || tz > 0 || ty > 0;
-#pragma unroll
-						for (int tx = 0; tx < 3; ++tx) {
-							const int t = tx + 3 * ty + 9 * tz;
-							const uint64_t bd = tc::smem_desc(b_base + static_cast<uint32_t>(t * 2 * N * 16), N * 16, 128);
-							tc::mma_bf16(tmem + static_cast<uint32_t>((zb * 3 + tx) * N), ad, bd, idesc, acc);
-						}
+						const int tyz = ty + 3 * tz;
+						const uint64_t bd = tc::smem_desc(b_base + static_cast<uint32_t>(tyz * 2 * 3 * N * 16), 3 * N * 16, 128);
+						tc::mma_bf16(tmem + static_cast<uint32_t>(zb * 3 * N), ad, bd, idesc, acc);
 					}
 				}
 			}
 			tc::commit(&empty[s]);
-			// the previous step's stage is free once its MMAs finish: refill it
-			if (p >= 1 && p - 1 + STAGES < a.steps) {
-				const int sp = (p - 1) % STAGES;
-				if (ok && !mbar_wait_bounded(&empty[sp], ((p - 1) / STAGES) & 1)) {
+			// A stage is free once the MMAs reading it finish. Two stages: refill the previous
+			// step's stage while this step's MMAs run. One stage: wait for this step's MMAs.
+			const int q = S == 1 ? p : p - 1;
+			if (q >= 0 && q + S < a.steps) {
+				const int sq = q % S;
+				if (ok && !mbar_wait_bounded(&empty[sq], (q / S) & 1)) {
 					ok = false;
 					report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 				}
-				load(p - 1 + STAGES);
+				load(q + S);
 			}
 		}
 		tc::commit(done);
@@ -204,8 +211,8 @@ __global__ void __launch_bounds__(128) cnn_tc_conv_kernel(const __grid_constant_
 	if (warp == 0) tc::tmem_dealloc(tmem, COLS);
 }
 
-// packed[s][t][h][n][k] = w[n][ci][t] with ci the (8 h + k)-th channel of step s: steps
-// 0 .. steps0 - 1 cover x0's channels 16 s .., the rest x1's (channel index c0 + ...).
+// packed[s][tyz][h][tx][n][k] = w[n][ci][tx + 3 tyz] with ci the (8 h + k)-th channel of
+// step s: steps 0 .. steps0 - 1 cover x0's channels 16 s .., the rest x1's (index c0 + ...).
 __global__ void pack_kernel(const uint16_t* w, int co, int c0, int c1, int n_pad, int steps0, int steps, uint16_t* packed)
 {
 	const long long n = static_cast<long long>(steps) * 27 * 2 * n_pad * 8;
@@ -214,8 +221,10 @@ __global__ void pack_kernel(const uint16_t* w, int co, int c0, int c1, int n_pad
 	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
 		const int k = static_cast<int>(i % 8);
 		const int nn = static_cast<int>((i / 8) % n_pad);
-		const int h = static_cast<int>((i / (8LL * n_pad)) % 2);
-		const int t = static_cast<int>((i / (16LL * n_pad)) % 27);
+		const int tx = static_cast<int>((i / (8LL * n_pad)) % 3);
+		const int h = static_cast<int>((i / (24LL * n_pad)) % 2);
+		const int tyz = static_cast<int>((i / (48LL * n_pad)) % 9);
+		const int t = tx + 3 * tyz;
 		const int s = static_cast<int>(i / (16LL * n_pad * 27));
 		const int local = 16 * (s < steps0 ? s : s - steps0) + 8 * h + k;
 		const int ci = s < steps0 ? (local < c0 ? local : -1) : (local < c1 ? c0 + local : -1);
@@ -233,11 +242,17 @@ int launch(const CUtensorMap& m0, const CUtensorMap& m1, const TcConvArgs& a, cu
 	static bool configured = false;
 	if (!configured) {
 		IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			static_cast<int>(smem_total(N, BZ))), "cnn_conv3_tc: shared memory attribute");
+			static_cast<int>(smem_total(N, BZ, MAX_STAGES))), "cnn_conv3_tc: shared memory attribute");
 		configured = true;
 	}
+	// Co-resident CTAs per SM are bounded by TMEM (512 columns per SM): ask for enough shared
+	// memory that no more CTAs than that land on an SM (228 KB per SM, 1 KB reserved per CTA).
+	const int per_sm = 512 / tmem_cols(N, BZ);
+	const size_t floor_bytes = 228 * 1024 / (per_sm + 1) - 1024 + 16;
+	size_t smem = smem_total(N, BZ, a.stages);
+	if (smem < floor_bytes) smem = floor_bytes;
 	const dim3 grid(static_cast<unsigned>(a.tiles_x * a.tiles_y), static_cast<unsigned>((a.d + BZ - 1) / BZ));
-	kernel<<<grid, 128, smem_total(N, BZ), st>>>(m0, m1, a);
+	kernel<<<grid, 128, smem, st>>>(m0, m1, a);
 	IANE_GB_CUDA(cudaGetLastError(), "cnn_conv3_tc: launch");
 	return IANE_GB_OK;
 }
@@ -290,7 +305,7 @@ int iane_gb_cnn_conv3_tc(const uint16_t* x0, int c0, const uint16_t* x1, int c1,
 		return fail(IANE_GB_INVALID_ARGUMENT, "cnn_conv3_tc: buffers must be 16-byte aligned");
 	}
 	const int n_pad = n_pad_of(co);
-	const int bz = n_pad == 16 ? 4 : 2;
+	const int bz = 2;
 	int* status = device_status_ptr();
 	if (!status) return IANE_GB_CUDA_ERROR;
 	CUtensorMap m0{}, m1{};
@@ -313,11 +328,12 @@ int iane_gb_cnn_conv3_tc(const uint16_t* x0, int c0, const uint16_t* x1, int c1,
 	a.act = act;
 	a.tiles_x = (w + OUT_X - 1) / OUT_X;
 	a.tiles_y = (h + TY - 1) / TY;
+	a.stages = a.steps > 1 ? 2 : 1;
 	a.status = status;
 	if ((d + bz - 1) / bz > 65535) return fail(IANE_GB_UNSUPPORTED, "cnn_conv3_tc: volume too deep");
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	switch (n_pad) {
-	case 16: return launch<16, 4>(m0, m1, a, st);
+	case 16: return launch<16, 2>(m0, m1, a, st);
 	case 32: return launch<32, 2>(m0, m1, a, st);
 	default: return launch<64, 2>(m0, m1, a, st);
 	}

@@ -557,6 +557,10 @@ def main(argv=None):
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--seed", type=int, default=0)
     t.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    f = sub.add_parser("forward", help="time the tensor-core forward of the shipped network")
+    f.add_argument("--shape", type=int, nargs=3, default=[64, 256, 256], metavar=("D", "H", "W"))
+    f.add_argument("--reps", type=int, default=3)
+    f.add_argument("--simt", action="store_true", help="use the SIMT kernels instead")
     e = sub.add_parser("eval")
     e.add_argument("--weights", default=str(DEFAULT_WEIGHTS))
     e.add_argument("--seed", type=int, default=7)
@@ -576,6 +580,20 @@ def main(argv=None):
         print(f"trained in {time.time() - t0:.1f} s", flush=True)
         Path(a.out).parent.mkdir(parents=True, exist_ok=True)
         net.save(a.out)
+    elif a.cmd == "forward":
+        net = load_default("cuda")
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(0)
+        vol = torch.rand(tuple(a.shape), generator=gen, device="cuda") * 2.0
+        net.forward(vol, 2.0, tensor_cores=not a.simt)  # first call packs the weights
+        torch.cuda.synchronize()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(a.reps):
+            net.forward(vol, 2.0, tensor_cores=not a.simt)
+        stop.record()
+        torch.cuda.synchronize()
+        print(json.dumps({"shape": a.shape, "tensor_cores": not a.simt, "ms": start.elapsed_time(stop) / a.reps}))
     else:
         net = WarmStartNet("cuda")
         net.load(a.weights)

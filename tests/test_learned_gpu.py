@@ -388,3 +388,43 @@ def test_training_reduces_the_loss(cuda):
     train(net, pairs, epochs=25, lr=2e-3)
     after = total_loss()
     assert after < 0.7 * before, (before, after)
+
+
+def test_learned_start_gains_over_the_flat_start(cuda):
+    """The shipped weights on a held-out 64^3 volume: the network's start is much closer to
+    the 200-iteration FP32 result than the flat start, stays closer after 10 iterations (BF16
+    tensor-core RL from the learned start, FP32 from the flat start), and reaches a relative
+    change of 1e-3 per iteration in far fewer iterations."""
+    import torch
+
+    import iane_gb300
+    from iane_gb300.learned import load_default, make_pair
+
+    net = load_default(cuda)
+    observed, sigma, target, psf = make_pair(np.random.default_rng(987654), size=64)
+    flat = torch.full_like(observed, float(observed.double().mean()))
+    start = net.warm_start(observed, sigma)
+    e_flat0, e_learn0 = _rel_l2(flat.cpu(), target.cpu()), _rel_l2(start.cpu(), target.cpu())
+    assert e_learn0 < 0.3 * e_flat0, (e_learn0, e_flat0)
+
+    rl32 = iane_gb300.RichardsonLucy(psf, observed.shape)
+    rl16 = iane_gb300.RichardsonLucy(psf, observed.shape, precision="bf16")
+    est32, est16 = torch.empty_like(observed), start.clone()
+    rl32.run(observed, est32, 10, 1e-6, init=rl32.INIT_MEAN)
+    rl16.run(observed, est16, 10, 1e-6, init=rl16.INIT_GIVEN)
+    e_plain10, e_learn10 = _rel_l2(est32.cpu(), target.cpu()), _rel_l2(est16.cpu(), target.cpu())
+    assert e_learn10 < 0.5 * e_plain10, (e_learn10, e_plain10)
+
+    def iterations_to_converge(rl, est, init):
+        stats = torch.zeros(2, dtype=torch.float64, device=cuda)
+        for k in range(1, 201):
+            rl.run(observed, est, 1, 1e-6, init=init if k == 1 else rl.INIT_GIVEN, stats=stats)
+            if float(stats[1]) <= 1e-3:
+                return k
+        return 201
+
+    n_plain = iterations_to_converge(rl32, torch.empty_like(observed), rl32.INIT_MEAN)
+    n_learn = iterations_to_converge(rl16, start.clone(), rl16.INIT_GIVEN)
+    assert n_learn <= n_plain // 2, (n_learn, n_plain)
+    rl32.close()
+    rl16.close()
