@@ -289,6 +289,234 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	}
 }
 
+// Ring variant for radius <= 4 on 3-D volumes with a TMA-addressable source (the common
+// case). Same tile and stages, with the per-plane overhead taken out:
+//   * two planes per iteration: the 2 x (16 + 2R) x 16 axis-0 row segments of both are dealt
+//     out over the 256 threads together (3 or 2 each instead of 2 or 1), and two block
+//     barriers serve two planes;
+//   * the axis-2 window lives in a thread-private ring in shared memory of L >= K + 1 slots
+//     (a power of two: the slot of plane m is m & (L - 1)); K + 1 conflict-free 128-bit loads
+//     give both planes' outputs. No register rotation;
+//   * all taps are held in registers;
+//   * the clamp/mirror fix-up of out-of-image halo cells is a list of (cell, source cell)
+//     pairs built once per block -- the x/y geometry is the same for every plane. Only cells
+//     within R of the image are listed (the others feed no stored output); for images of at
+//     least 16 x 16 their source cells lie inside the tile;
+//   * only the thread that issues a plane's TMA maps its z coordinate.
+constexpr int kRBuf = 3; // tile buffers: the iteration's two planes and the next one
+
+template<int R>
+struct RingGeom {
+	using G = SepGeom<R>;
+	static constexpr int L = R == 1 ? 4 : (R <= 3 ? 8 : 16);   // ring slots, >= K + 1
+	static constexpr int FIX = 2 * R * (G::AW + G::AH);        // out-of-image cells within R of the image
+	static constexpr int SEGS = G::AH * (kFX / 4);              // axis-0 row segments of one plane
+	static constexpr size_t BYTES = static_cast<size_t>(kRBuf * G::A_FLOATS + 2 * G::B_FLOATS) * 4 +
+		static_cast<size_t>(L) * kFThreads * 16 + static_cast<size_t>(FIX) * 4 + kRBuf * 8 + 16;
+};
+
+template<int R>
+__global__ void __launch_bounds__(kFThreads, R <= 3 ? 3 : 2) separable_ring_kernel(
+	const __grid_constant__ CUtensorMap map, const SepFastArgs a)
+{
+	using G = SepGeom<R>;
+	using RG = RingGeom<R>;
+	constexpr int K = G::K;
+	constexpr int L = RG::L;
+	constexpr int FIX = RG::FIX;
+	constexpr int SEGS = RG::SEGS;
+	static_assert(L >= K + 1 && (L & (L - 1)) == 0, "ring length");
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	float* A = reinterpret_cast<float*>(smem_raw);                              // kRBuf tiles
+	float* Bbuf = A + kRBuf * G::A_FLOATS;                                       // axis-0 results, 2 planes
+	float4* ring = reinterpret_cast<float4*>(Bbuf + 2 * G::B_FLOATS);            // [L][threads]
+	uint32_t* fix = reinterpret_cast<uint32_t*>(ring + L * kFThreads);           // (cell << 16) | source
+	uint64_t* bars = reinterpret_cast<uint64_t*>(fix + FIX);
+	int* nfix_s = reinterpret_cast<int*>(bars + kRBuf);
+
+	const int tid = threadIdx.x;
+	const int x0 = blockIdx.x * kFX, y0 = blockIdx.y * kFY;
+	const int zs = blockIdx.z * a.zchunk;
+	const int ze = min(zs + a.zchunk, a.nz);
+	const int nplanes = (ze - zs) + 2 * R;
+	const int npairs = (nplanes + 1) / 2;   // an odd count reads one extra plane, never stored
+	const bool interior = x0 - G::RA >= 0 && x0 + kFX + G::RA <= a.nx && y0 - R >= 0 && y0 + kFY + R <= a.ny;
+	const bool fixup = !interior && a.border != IANE_GB_BORDER_ZERO;
+
+	auto tap = [&](int axis, int i) -> float {
+		if (!a.tap_ptr[axis]) {
+			return i == R ? 1.0f : 0.0f;
+		}
+		const int q = i - (R - a.k[axis] / 2);
+		return q >= 0 && q < a.k[axis] ? *reinterpret_cast<const float*>(a.tap_ptr[axis] + q * a.tap_stride[axis])
+			: 0.0f;
+	};
+	float tx[K];
+	float2 ty2[K], tz2[K];
+#pragma unroll
+	for (int i = 0; i < K; ++i) {
+		tx[i] = tap(0, i);
+		const float t1 = tap(1, i), t2 = tap(2, i);
+		ty2[i] = make_float2(t1, t1);
+		tz2[i] = make_float2(t2, t2);
+	}
+	if (tid == 0) {
+		*nfix_s = 0;
+		for (int b = 0; b < kRBuf; ++b) mbar_init(&bars[b], 1);
+		fence_barrier_init();
+	}
+	__syncthreads();
+	if (fixup) {
+		const int gx0 = x0 - G::RA, gy0 = y0 - R;
+		for (int i = tid; i < G::AW * G::AH; i += kFThreads) {
+			const int r = i / G::AW, c = i - r * G::AW;
+			const int gx = gx0 + c, gy = gy0 + r;
+			const int dx = gx < 0 ? -gx : (gx >= a.nx ? gx - a.nx + 1 : 0);
+			const int dy = gy < 0 ? -gy : (gy >= a.ny ? gy - a.ny + 1 : 0);
+			if ((dx == 0 && dy == 0) || dx > R || dy > R) continue;
+			int mx = 0, my = 0;
+			map_coord(gx, a.nx, a.border, mx);
+			map_coord(gy, a.ny, a.border, my);
+			const int lc = mx - gx0, lr = my - gy0;
+			if (lc < 0 || lc >= G::AW || lr < 0 || lr >= G::AH) continue; // cannot happen for images >= 16 x 16
+			const int k = atomicAdd(nfix_s, 1);
+			if (k < FIX) fix[k] = (static_cast<uint32_t>(i) << 16) | static_cast<uint32_t>(lr * G::AW + lc);
+		}
+	}
+	__syncthreads();
+	const int nfix = min(*nfix_s, FIX);
+
+	// plane m of the sequence is input plane zs - R + m, in tile buffer m % kRBuf; thread 0 issues
+	auto issue = [&](int m) {
+		const int b = m % kRBuf;
+		const int z = zs - R + m;
+		int zi = 0;
+		const bool present = map_coord(z, a.nz, a.border, zi);
+		if (fixup) {
+			// order this buffer's earlier generic-proxy writes (the fix-up) before the TMA
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+		}
+		mbar_arrive_expect_tx(&bars[b], static_cast<uint32_t>(G::AW * G::AH * 4));
+		tma_load_3d(A + b * G::A_FLOATS, &map, x0 - G::RA, y0 - R, present ? zi : z, &bars[b]);
+	};
+	if (tid == 0) {
+		issue(0);
+		issue(1);
+	}
+	bool ok = true;
+	auto wait_fix = [&](int m) {
+		const int b = m % kRBuf;
+		if (ok && !mbar_wait_bounded(&bars[b], (m / kRBuf) & 1)) {
+			ok = false;
+			report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
+		}
+		float* tile = A + b * G::A_FLOATS;
+		for (int k = tid; k < nfix; k += kFThreads) {
+			const uint32_t e = fix[k];
+			tile[e >> 16] = tile[e & 0xFFFFu];
+		}
+	};
+
+	const int xp = tid & 31, yq = tid >> 5;   // axes 1, 2: x pair 2xp, y rows 2yq, 2yq + 1
+	const int ox = x0 + 2 * xp, oy = y0 + 2 * yq;
+	const bool pairs = a.dst_pairs && ox + 1 < a.nx;
+	char* row0 = a.dst + oy * a.d_stride[1] + ox * a.d_stride[0];
+	char* row1 = row0 + a.d_stride[1];
+	const bool y0_in = oy < a.ny, y1_in = oy + 1 < a.ny, x0_in = ox < a.nx, x1_in = ox + 1 < a.nx;
+	float4* my_ring = ring + tid;
+
+	auto store = [&](int zo, const float2& o0, const float2& o1) {
+		const long long zoff = static_cast<long long>(zo) * a.d_stride[2];
+		if (pairs) {
+			if (y0_in) *reinterpret_cast<float2*>(row0 + zoff) = o0;
+			if (y1_in) *reinterpret_cast<float2*>(row1 + zoff) = o1;
+		} else {
+			if (y0_in && x0_in) *reinterpret_cast<float*>(row0 + zoff) = o0.x;
+			if (y0_in && x1_in) *reinterpret_cast<float*>(row0 + zoff + a.d_stride[0]) = o0.y;
+			if (y1_in && x0_in) *reinterpret_cast<float*>(row1 + zoff) = o1.x;
+			if (y1_in && x1_in) *reinterpret_cast<float*>(row1 + zoff + a.d_stride[0]) = o1.y;
+		}
+	};
+
+	for (int pp = 0; pp < npairs; ++pp) {
+		const int p = 2 * pp; // planes p and p + 1
+		// plane p + 2 goes to the buffer of plane p - 1, whose axis-0 reads ended before the
+		// first barrier of the previous iteration. Only planes this block waits for are
+		// issued: no copy may still be in flight when the block exits.
+		if (tid == 0 && p + 2 < 2 * npairs) issue(p + 2);
+		wait_fix(p);
+		wait_fix(p + 1);
+		if (nfix > 0) __syncthreads(); // fixed tiles visible to all
+		// axis 0 of both planes into B[0], B[1]: segment it = (plane, row, 4-column group);
+		// B's last readers (axis 1 of the previous iteration) finished before its second barrier
+		for (int it = tid; it < 2 * SEGS; it += kFThreads) {
+			const int pl = it >= SEGS ? 1 : 0;
+			const int rem = it - pl * SEGS;
+			const int r = rem >> 4, xq = rem & 15;
+			const float* tile = A + ((p + pl) % kRBuf) * G::A_FLOATS;
+			float seg[G::SEG];
+			const float4* srow = reinterpret_cast<const float4*>(tile + r * G::AW + 4 * xq);
+#pragma unroll
+			for (int m = 0; m < G::SEG / 4; ++m) {
+				const float4 v = srow[m];
+				seg[4 * m] = v.x;
+				seg[4 * m + 1] = v.y;
+				seg[4 * m + 2] = v.z;
+				seg[4 * m + 3] = v.w;
+			}
+			float o[4];
+#pragma unroll
+			for (int i = 0; i < 4; ++i) {
+				float acc = 0.0f;
+#pragma unroll
+				for (int q = 0; q < K; ++q) acc = fmaf(tx[q], seg[G::D + i + 2 * R - q], acc);
+				o[i] = acc;
+			}
+			*reinterpret_cast<float4*>(Bbuf + pl * G::B_FLOATS + r * kFX + 4 * xq) = make_float4(o[0], o[1], o[2], o[3]);
+		}
+		__syncthreads(); // B complete; the tiles of planes p, p + 1 are free
+		// plane p + 3 goes to the buffer of plane p, just released
+		if (tid == 0 && p + 3 < 2 * npairs) issue(p + 3);
+#pragma unroll
+		for (int pl = 0; pl < 2; ++pl) {
+			const float* B = Bbuf + pl * G::B_FLOATS;
+			float2 c0 = make_float2(0.0f, 0.0f), c1 = make_float2(0.0f, 0.0f);
+			float2 col[2 + 2 * R];
+#pragma unroll
+			for (int m = 0; m < 2 + 2 * R; ++m) {
+				col[m] = *reinterpret_cast<const float2*>(B + (2 * yq + m) * kFX + 2 * xp);
+			}
+#pragma unroll
+			for (int q = 0; q < K; ++q) {
+				c0 = __ffma2_rn(col[2 * R - q], ty2[q], c0);
+				c1 = __ffma2_rn(col[1 + 2 * R - q], ty2[q], c1);
+			}
+			my_ring[((p + pl) & (L - 1)) * kFThreads] = make_float4(c0.x, c0.y, c1.x, c1.y);
+		}
+		__syncthreads(); // both B buffers read: the next iteration may overwrite them
+		if (p + 1 >= 2 * R) {
+			// output planes zs + p - 2R and zs + p + 1 - 2R; tap q meets planes p - q, p + 1 - q
+			float2 a0 = make_float2(0.0f, 0.0f), a1 = make_float2(0.0f, 0.0f);   // plane p + 1's output
+			float2 b0 = make_float2(0.0f, 0.0f), b1 = make_float2(0.0f, 0.0f);   // plane p's output
+#pragma unroll
+			for (int j = 0; j <= K; ++j) {
+				const float4 v = my_ring[((p + 1 - j) & (L - 1)) * kFThreads]; // plane p + 1 - j
+				if (j < K) {
+					a0 = __ffma2_rn(make_float2(v.x, v.y), tz2[j], a0);
+					a1 = __ffma2_rn(make_float2(v.z, v.w), tz2[j], a1);
+				}
+				if (j >= 1) {
+					b0 = __ffma2_rn(make_float2(v.x, v.y), tz2[j - 1], b0);
+					b1 = __ffma2_rn(make_float2(v.z, v.w), tz2[j - 1], b1);
+				}
+			}
+			const int zo = zs + p - 2 * R;
+			if (p >= 2 * R && zo < ze) store(zo, b0, b1);
+			if (zo + 1 < ze) store(zo + 1, a0, a1);
+		}
+	}
+}
+
 template<int R>
 int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, int border, cudaStream_t stream)
 {
@@ -336,6 +564,16 @@ int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, i
 	const size_t smem = (kNBuf * G::A_FLOATS + G::B_FLOATS) * sizeof(float) + 2 * 16 * sizeof(float2) +
 		kNBuf * sizeof(uint64_t);
 	const dim3 grid((a.nx + kFX - 1) / kFX, (a.ny + kFY - 1) / kFY, z3 ? (a.nz + chunk - 1) / chunk : 1);
+	if constexpr (R <= 4) {
+		if (z3 && a.use_tma && a.nx >= 16 && a.ny >= 16) {
+			const size_t rsmem = RingGeom<R>::BYTES;
+			IANE_GB_CUDA(cudaFuncSetAttribute(separable_ring_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				static_cast<int>(rsmem)), "separable: set shared memory size");
+			separable_ring_kernel<R><<<grid, kFThreads, rsmem, stream>>>(map, a);
+			IANE_GB_CUDA(cudaGetLastError(), "separable: launch");
+			return IANE_GB_OK;
+		}
+	}
 	if (z3) {
 		IANE_GB_CUDA(cudaFuncSetAttribute(separable_fast_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			static_cast<int>(smem)), "separable: set shared memory size");

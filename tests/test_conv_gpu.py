@@ -181,7 +181,8 @@ def test_rl_volume_convolution_slabs(cuda):
 @pytest.mark.parametrize("shape,taps", [((40,), (7,)), ((33, 70), (7, 7)), ((512, 512), (7, 7)), ((9, 30, 75), (5, 3, 7)),
                                        ((20, 20, 20), (9, 9, 9)), ((3, 5, 4), (7, 9, 11)), ((70, 90), (21, 3)),
                                        ((37, 41, 130), (15, 15, 15)), ((1, 1, 1), (3, 3, 3)), ((17, 1, 200), (3, 5, 1)),
-                                       ((64, 64, 64), (3, 3, 3))])
+                                       ((64, 64, 64), (3, 3, 3)), ((50, 70, 150), (7, 7, 7)), ((33, 17, 16), (9, 1, 5)),
+                                       ((130, 40, 66), (3, 7, 9)), ((12, 16, 16), (5, 5, 5))])
 def test_separable_parity(cuda, shape, taps, border):
     rng = np.random.default_rng(len(shape) * 100 + taps[0])
     src = rng.random(shape, dtype=np.float32)
