@@ -180,11 +180,13 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def measure_hbm_legs(dev, stream, reps=20):
+def measure_hbm_legs(dev, stream, reps=20, cpu=True):
     """HBM-bound convolutions beside the main workload: the fused separable kernel on a
-    512^3 f32 volume (7-tap Gaussians, mirror border; 1 GiB in + out, larger than L2) and
-    the 2-D 512x512 7x7 Gaussian mirror case, direct and separable. Device time per launch
-    (CUDA events), algorithmic bytes = 8 per voxel (one read, one write)."""
+    512^3 f32 volume (7-tap Gaussians, mirror border; 1 GiB in + out, larger than L2), the
+    2-D 512x512 7x7 Gaussian mirror configuration, direct and separable (with the host
+    baseline: the oracle port of the reference's convolve on all host threads and on one),
+    and the same 2-D filter at 8192x8192 where bandwidth can be judged. Device time per
+    launch (CUDA events), algorithmic bytes = 8 per voxel (one read, one write)."""
     import numpy as np
     import torch
 
@@ -224,6 +226,40 @@ def measure_hbm_legs(dev, stream, reps=20):
     out["direct_512^2_7x7_mirror"] = {"ms": ms, "gvoxel_s": img.numel() / (ms / 1e3) / 1e9}
     ms = timed(lambda: iane_gb300.convolve_separable(img, [g1, g1], d2, "mirror", stream=stream))
     out["separable_512^2_7x7_mirror"] = {"ms": ms, "gvoxel_s": img.numel() / (ms / 1e3) / 1e9}
+    if cpu:
+        # the 2-D configuration on the host: the reference's convolve (oracle port) with all
+        # host threads and with one
+        import oracle
+        from oracle import build as oracle_build
+
+        oracle_build.build_oracle()
+        src_np = img.cpu().numpy()
+        k_np = g2.cpu().numpy()
+        ref_np = np.zeros_like(src_np)
+        for threads in (oracle.default_threads(), 1):
+            oracle.convolve(src_np, k_np, ref_np, "mirror", threads=threads)
+            t0 = time.perf_counter()
+            n = 0
+            while time.perf_counter() - t0 < 1.0:
+                oracle.convolve(src_np, k_np, ref_np, "mirror", threads=threads)
+                n += 1
+            cms = (time.perf_counter() - t0) / n * 1e3
+            key = "cpu_baseline_all_threads" if threads > 1 else "cpu_baseline_1_thread"
+            out["direct_512^2_7x7_mirror"][key] = {"ms": cms, "cores": threads, "kind": "port",
+                                                   "gvoxel_s": img.numel() / (cms / 1e3) / 1e9}
+        out["direct_512^2_7x7_mirror"]["gpu_speedup_vs_all_threads"] = (
+            out["direct_512^2_7x7_mirror"]["cpu_baseline_all_threads"]["ms"] / out["direct_512^2_7x7_mirror"]["ms"])
+    del img, d2
+    # bandwidth at a large 2-D size (256 MiB in, 256 MiB out: larger than L2)
+    big = torch.rand((8192, 8192), generator=gen, device=dev, dtype=torch.float32)
+    dbig = torch.empty_like(big)
+    for name, fn in (("direct_8192^2_7x7_mirror", lambda: iane_gb300.convolve(big, g2, dbig, "mirror", stream=stream)),
+                     ("separable_8192^2_7x7_mirror",
+                      lambda: iane_gb300.convolve_separable(big, [g1, g1], dbig, "mirror", stream=stream))):
+        ms = timed(fn)
+        gbs = 8.0 * big.numel() / (ms / 1e3) / 1e9
+        out[name] = {"ms": ms, "gvoxel_s": big.numel() / (ms / 1e3) / 1e9, "gbs": gbs, "hbm_frac": gbs / hbm}
+    del big, dbig
     return out
 
 
@@ -261,6 +297,15 @@ def measure_bf16_leg(dev, stream, reps=5):
         results[precision] = est.double()
         out[precision] = {"ms_per_run": ms, "gvoxel_s": 2 * ITERATIONS * observed.size / (ms / 1e3) / 1e9,
                           "tflops_useful": 2 * ITERATIONS * observed.size * 2 * psf.size / (ms / 1e3) / 1e12}
+        if precision == "bf16":
+            # banded-Toeplitz GEMMs: per output voxel and kernel row (ky x kz rows), an MMA
+            # slice of K = 32 input columns for 16 outputs, i.e. 32 issued MACs per output
+            kz, ky, kx = psf.shape
+            issued = 32 * ky * kz
+            out[precision]["issued_macs_per_voxel_conv"] = issued
+            out[precision]["useful_macs_per_voxel_conv"] = kx * ky * kz
+            out[precision]["useful_mac_fraction"] = kx * ky * kz / issued
+            out[precision]["tflops_issued"] = out[precision]["tflops_useful"] * issued / (kx * ky * kz)
         rl.close()
     d = results["bf16"] - results["f32"]
     out["bf16_vs_f32"] = {"rel_l2": float(d.norm() / results["f32"].norm()), "max_abs": float(d.abs().max()),
@@ -269,7 +314,7 @@ def measure_bf16_leg(dev, stream, reps=5):
     return out
 
 
-def measure_batch_leg(dev, stream, reps=3, iterations=30):
+def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     """Batched uneven 2-D RL: 256 images, sides log-uniform in [64, 1024], own Gaussian PSF
     each (odd size 3-31, sigma 0.5-5), Poisson noise, 30 iterations, one CUDA-graph replay
     per run of persistent work-queue passes, autotuned tile shapes."""
@@ -309,10 +354,35 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30):
     widths = batch.tile_widths()
     batch.close()
     assert all(bool(torch.isfinite(o).all()) for o in outs)
-    return {"images": len(obs), "pixels": pixels, "iterations": iterations, "ms_per_run": ms,
-            "gvoxel_s": 2 * iterations * pixels / (ms / 1e3) / 1e9, "tflops_useful": 2 * macs / (ms / 1e3) / 1e12,
-            "tiles_64": int(sum(1 for w in widths if w == 64)), "tiles_32": int(sum(1 for w in widths if w == 32)),
-            "prepare_s": prepare_s}
+    peaks, _ = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    fp32 = 152 * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    alg_bytes = 24.0 * pixels * iterations   # per iteration: pass A 12 B/px, pass B 12 B/px
+    res = {"images": len(obs), "pixels": pixels, "iterations": iterations, "ms_per_run": ms,
+           "gvoxel_s": 2 * iterations * pixels / (ms / 1e3) / 1e9, "tflops_useful": 2 * macs / (ms / 1e3) / 1e12,
+           "gbs_algorithmic": alg_bytes / (ms / 1e3) / 1e9,
+           "tiles_64": int(sum(1 for w in widths if w == 64)), "tiles_32": int(sum(1 for w in widths if w == 32)),
+           "prepare_s": prepare_s}
+    res["frac_of_fp32_peak"] = res["tflops_useful"] / fp32
+    res["frac_of_hbm_peak"] = res["gbs_algorithmic"] / hbm
+    if cpu:
+        # the reference's RL loop (oracle port, all host threads) on the first 8 images
+        import oracle
+        from oracle import build as oracle_build
+
+        oracle_build.build_oracle()
+        threads = oracle.default_threads()
+        sample = list(range(8))
+        o_np = [obs[i].cpu().numpy() for i in sample]
+        t0 = time.perf_counter()
+        for i, o in zip(sample, o_np):
+            oracle.rl(o, psfs[i], iterations, EPSILON, init=oracle.abi.RL_INIT_MEAN, threads=threads)
+        dt = time.perf_counter() - t0
+        px = sum(o.size for o in o_np)
+        res["cpu_baseline"] = {"value": 2 * iterations * px / dt / 1e9, "unit": "GVoxel/s", "cores": threads,
+                               "kind": "port", "sample": f"oracle RL, {iterations} iterations, first 8 images "
+                                                         f"({px} pixels, {dt:.1f} s)"}
+    return res
 
 
 def measure_learned_leg(dev):
@@ -420,9 +490,10 @@ def main():
         e2e_s = float(t.item())
     e2e_value = world * conv_voxels_per_step * e2e_steps / e2e_s / 1e9
 
-    hbm_legs = measure_hbm_legs(dev, stream)
+    with_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
+    hbm_legs = measure_hbm_legs(dev, stream, cpu=with_cpu)
     bf16_leg = measure_bf16_leg(dev, stream)
-    batch_leg = measure_batch_leg(dev, stream)
+    batch_leg = measure_batch_leg(dev, stream, cpu=with_cpu)
     learned_leg = measure_learned_leg(dev)
 
     # result sanity: the run converged to something finite and positive

@@ -7,9 +7,10 @@
 //     (32 WX) x (32 WY) outputs;
 //   * for each kernel plane qz the input halo tile of that plane, (TX + 2 rx) x (TY + 2 ry)
 //     floats, is staged in shared memory -- by one TMA (cp.async.bulk.tensor, zero fill
-//     outside the image) when the border is zero and the buffer is TMA-addressable, else by
-//     4-byte cp.async with the border rule applied per element -- double buffered, so the
-//     next plane lands while this one is consumed;
+//     outside the image; for clamp and mirror borders, tiles at the image edge then rewrite
+//     their out-of-image cells from the cells the rule maps them to) when the buffer is
+//     TMA-addressable, else by 4-byte cp.async with the border rule applied per element --
+//     double buffered, so the next plane lands while this one is consumed;
 //   * a lane walks the RY + 2 ry input rows it needs; each row segment (8 + 2 rx floats) is
 //     read once with 128-bit shared loads into registers and feeds every (output row j,
 //     kernel row b) pair that uses it: 8 x KX FMAs per (j, b) against a kernel row that is
@@ -135,10 +136,14 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 		const int qz = qz_lo + p;
 		if constexpr (TMA) {
 			if (tid == 0) {
+				// zero border: an out-of-volume plane is never issued (qz range above); clamp
+				// and mirror: the plane the rule maps to
+				int zi = z + rz - qz;
+				if (a.border != IANE_GB_BORDER_ZERO) map_coord(z + rz - qz, a.nz, a.border, zi);
 				// order earlier generic-proxy use of this buffer before the async-proxy write
 				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 				mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(P * H * 4));
-				tma_load_3d(dst, tmap_ptr, x0 - G::RXA, y0 - ry, z + rz - qz, &bars[p & 1]);
+				tma_load_3d(dst, tmap_ptr, x0 - G::RXA, y0 - ry, zi, &bars[p & 1]);
 			}
 		} else {
 			int zi = 0;
@@ -163,6 +168,12 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 		for (int i = 0; i < kRX; ++i) acc[j][i] = 0.0f;
 
 	bool ok = true;
+	// TMA with a clamp or mirror border: a tile that reaches outside the image gets its
+	// out-of-image cells within (rx, ry) of the image -- the only ones stored outputs read --
+	// from the in-image cells the rule maps them to. Those lie inside the tile whenever
+	// nx > rx and ny > ry (the launcher's condition); any other cell keeps the TMA's zeros.
+	const bool fix_tile = TMA && a.border != IANE_GB_BORDER_ZERO &&
+		!(x0 - G::RXA >= 0 && x0 - G::RXA + W <= a.nx && y0 - ry >= 0 && y0 + TY + ry <= a.ny);
 	if (nplanes > 0) issue(0);
 	if (nplanes > 1) issue(1);
 	for (int p = 0; p < nplanes; ++p) {
@@ -173,6 +184,24 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
 			phases ^= bit;
+			if (fix_tile) {
+				float* t = tiles + (p & 1) * plane_floats;
+				const int gx0 = x0 - G::RXA, gy0 = y0 - ry;
+				for (int i = tid; i < W * H; i += NT) {
+					const int r = i / W, c = i - r * W;
+					const int gx = gx0 + c, gy = gy0 + r;
+					const int dx = gx < 0 ? -gx : (gx >= a.nx ? gx - a.nx + 1 : 0);
+					const int dy = gy < 0 ? -gy : (gy >= a.ny ? gy - a.ny + 1 : 0);
+					if ((dx == 0 && dy == 0) || dx > G::rx || dy > ry) continue;
+					int mx = 0, my = 0;
+					map_coord(gx, a.nx, a.border, mx);
+					map_coord(gy, a.ny, a.border, my);
+					const int lc = mx - gx0, lr = my - gy0;
+					if (lc < 0 || lc >= W || lr < 0 || lr >= H) continue;
+					t[r * P + c] = t[lr * P + lc];
+				}
+				__syncthreads(); // fixed tile visible to all lanes
+			}
 		} else {
 			if (p + 1 < nplanes) {
 				cp_async_wait<1>();

@@ -104,6 +104,8 @@ SHAPES = [
     ((1, 1), (3, 3)), ((17, 29), (5, 7)), ((64, 64), (7, 7)), ((70, 131), (15, 31)), ((3, 200), (9, 1)),
     ((1, 1, 1), (3, 3, 3)), ((9, 10, 11), (3, 5, 7)), ((7, 33, 65), (7, 15, 15)), ((4, 5, 6), (9, 9, 9)),
     ((19, 40, 72), (5, 3, 13)), ((2, 96, 100), (3, 11, 21)),
+    # 16-byte aligned rows: TMA staging, clamp/mirror edges fixed up in shared memory
+    ((9, 8), (15, 15)), ((16, 24), (13, 31)), ((5, 12, 20), (7, 9, 5)), ((3, 130, 260), (3, 7, 7)),
 ]
 
 
