@@ -12,7 +12,7 @@
 //   misc   : block-completion counter and the flat-start value
 #include "kernels.h"
 #include "rl.cuh"
-#include "rl_tc.cuh"
+#include "rl_tcz.cuh"
 #include "rl_batch.cuh"
 
 #include <cmath>
@@ -44,6 +44,7 @@ struct iane_gb_rl_plan {
 	__nv_bfloat16* d_tmat_adj;
 	long long pitch16;         // bf16 elements per work-image row (multiple of 8)
 	size_t image16_bytes;
+	bool tcz;                  // z planes along N (rl_tcz.cuh); T matrices in its layout
 };
 
 namespace iane_gb {
@@ -325,7 +326,7 @@ int rl_run_bf16(iane_gb_rl_plan* plan, const DevView& obs, const DevView& est, i
 	ta.ky = ky;
 	ta.kz = plan->k[2];
 	ta.status = dstatus;
-	ta.smem_bytes = static_cast<int>(tc_smem_bytes(ky));
+	ta.smem_bytes = static_cast<int>(plan->tcz ? tcz_smem_bytes(ky, plan->k[2]) : tc_smem_bytes(ky));
 	ta.tmem_cols = kTcTmemCols;
 	TcArgs tb = ta;
 	ta.tmat = plan->d_tmat_psf;
@@ -368,12 +369,12 @@ int rl_run_bf16(iane_gb_rl_plan* plan, const DevView& obs, const DevView& est, i
 	eb.out = est.ptr;
 	eb.out_u8 = est.dtype == IANE_GB_U8;
 	for (int it = 0; it < iterations; ++it) {
-		status = launch_tc_pass_a(map_est, ta, ea, st);
+		status = plan->tcz ? launch_tcz_pass_a(map_est, ta, ea, st) : launch_tc_pass_a(map_est, ta, ea, st);
 		if (status) return status;
 		eb.want_stats = stats != nullptr;
 		eb.stats = stats ? stats + 2 * it : nullptr;
 		eb.write_out = (!in_place && it == iterations - 1) ? 1 : 0;
-		status = launch_tc_pass_b(map_ratio, tb, eb, st);
+		status = plan->tcz ? launch_tcz_pass_b(map_ratio, tb, eb, st) : launch_tc_pass_b(map_ratio, tb, eb, st);
 		if (status) return status;
 	}
 	if (iterations == 0 && !in_place) {
@@ -642,8 +643,11 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 		return cleanup(cuda_fail(cudaGetLastError(), "rl_prepare: allocate sensitivity tables"));
 	}
 	if (bf16) {
-		// T_{b,qz}[k][n] = kernel[qz][b][n + rx + 8 - k], stored [qz][b][k / 8][n][k % 8]
+		// T_{b,qz}[k][n] = kernel[qz][b][n + rx + 8 - k], stored [qz][b][k / 8][n][k % 8] for
+		// tc_conv_kernel, or [b][k / 8][qz][n][k % 8] (all planes N-contiguous) for
+		// tcz_conv_kernel when they fit in its shared memory
 		const int kx = k.ext[0], ky = k.ext[1], kz = k.ext[2], rx = kx / 2;
+		plan->tcz = tcz_supported(kx, ky, kz);
 		const size_t per = static_cast<size_t>(kTcTmatBytes / 2);
 		std::vector<__nv_bfloat16> tp(static_cast<size_t>(kz) * ky * per), ta(tp.size());
 		for (int qz = 0; qz < kz; ++qz)
@@ -651,7 +655,9 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 				for (int kk = 0; kk < 32; ++kk)
 					for (int n = 0; n < 16; ++n) {
 						const int tap = n + rx + kTcXA - kk;
-						const size_t at = (static_cast<size_t>(qz) * ky + b) * per + (kk / 8) * 128 + n * 8 + kk % 8;
+						const size_t at = plan->tcz
+							? ((static_cast<size_t>(b) * 4 + kk / 8) * kz + qz) * 128 + n * 8 + kk % 8
+							: (static_cast<size_t>(qz) * ky + b) * per + (kk / 8) * 128 + n * 8 + kk % 8;
 						const size_t src = (static_cast<size_t>(qz) * ky + b) * kx + tap;
 						tp[at] = __float2bfloat16_rn(tap >= 0 && tap < kx ? h_psf[src] : 0.0f);
 						ta[at] = __float2bfloat16_rn(tap >= 0 && tap < kx ? h_adj[src] : 0.0f);
@@ -689,7 +695,9 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 		// scratch: f32 work estimate, bf16 estimate shadow, bf16 ratio, partials, counter
 		plan->pitch16 = (static_cast<long long>(ext[0]) + 7) & ~7LL;
 		plan->image16_bytes = round_up(static_cast<size_t>(plan->pitch16) * ext[1] * ext[2] * 2, kAlign);
-		plan->pass_blocks = static_cast<long long>((ext[0] + kTcN - 1) / kTcN) * ((ext[1] + kTcM - 1) / kTcM) * ext[2];
+		plan->pass_blocks = plan->tcz
+			? static_cast<long long>((ext[0] + 15) / 16) * ((ext[1] + kTcM - 1) / kTcM) * ((ext[2] + kTczZ - 1) / kTczZ)
+			: static_cast<long long>((ext[0] + kTcN - 1) / kTcN) * ((ext[1] + kTcM - 1) / kTcM) * ext[2];
 		plan->parts_bytes = round_up(static_cast<size_t>(
 			(plan->pass_blocks * 3 > mean_blocks ? plan->pass_blocks * 3 : mean_blocks) * sizeof(double)), kAlign);
 		plan->scratch_bytes = plan->image_bytes + 2 * plan->image16_bytes + plan->parts_bytes + 2 * kAlign;

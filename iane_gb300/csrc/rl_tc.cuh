@@ -188,22 +188,53 @@ struct EpiRatioTc {
 	float eps;
 	int nx, ny;
 
+	// one output voxel (x, y, z) with prediction pr
+	__device__ __forceinline__ void one(int xx, int y, int z, float pr) const
+	{
+		if (y >= ny || xx >= nx) return;
+		const char* q = obs + xx * os[0] + y * os[1] + z * os[2];
+		const float o = obs_u8 ? static_cast<float>(*reinterpret_cast<const uint8_t*>(q)) : *reinterpret_cast<const float*>(q);
+		ratio[z * plane + y * pitch + xx] = __float2bfloat16_rn(o / (pr > eps ? pr : eps));
+	}
+
 	// one warp, one row: this lane's columns x and x + 32
 	__device__ __forceinline__ void row_pair(int x, int y, int z, float p0, float p1) const
 	{
+		one(x, y, z, p0);
+		one(x + 32, y, z, p1);
+	}
+
+	// 16 consecutive outputs x0 .. x0 + 15 of row y (x0 a multiple of 16): vector loads and
+	// stores when the run lies inside the image and the observed row is f32 and aligned
+	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&pr)[16]) const
+	{
 		if (y >= ny) return;
-		__nv_bfloat16* out = ratio + z * plane + y * pitch;
-		const char* orow = obs + y * os[1] + z * os[2];
+		const char* orow = obs + y * os[1] + z * os[2] + x0 * os[0];
+		if (x0 + 16 <= nx && !obs_u8 && os[0] == 4 && (reinterpret_cast<uintptr_t>(orow) & 15) == 0) {
+			float o[16];
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
-			const int xx = x + 32 * h;
-			if (xx < nx) {
-				const char* q = orow + xx * os[0];
-				const float o = obs_u8 ? static_cast<float>(*reinterpret_cast<const uint8_t*>(q)) : *reinterpret_cast<const float*>(q);
-				const float pr = h ? p1 : p0;
-				out[xx] = __float2bfloat16_rn(o / (pr > eps ? pr : eps));
+			for (int q = 0; q < 4; ++q) {
+				const float4 v = *reinterpret_cast<const float4*>(orow + 16 * q);
+				o[4 * q] = v.x;
+				o[4 * q + 1] = v.y;
+				o[4 * q + 2] = v.z;
+				o[4 * q + 3] = v.w;
 			}
+			uint32_t w[8];
+#pragma unroll
+			for (int c = 0; c < 8; ++c) {
+				const float r0 = o[2 * c] / (pr[2 * c] > eps ? pr[2 * c] : eps);
+				const float r1 = o[2 * c + 1] / (pr[2 * c + 1] > eps ? pr[2 * c + 1] : eps);
+				const __nv_bfloat162 h = __floats2bfloat162_rn(r0, r1);
+				w[c] = *reinterpret_cast<const uint32_t*>(&h);
+			}
+			uint4* dst = reinterpret_cast<uint4*>(ratio + z * plane + y * pitch + x0);
+			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+			return;
 		}
+#pragma unroll
+		for (int c = 0; c < 16; ++c) one(x0 + c, y, z, pr[c]);
 	}
 	__device__ __forceinline__ void finish() const {}
 };
@@ -232,40 +263,91 @@ struct EpiUpdateTc {
 	int out_u8;
 	float f_s, f_c, c_s, c_c, n_s, n_c;
 
-	__device__ __forceinline__ void row_pair(int x, int y, int z, float c0, float c1)
+	// one output voxel (x, y, z) with correction cv
+	__device__ __forceinline__ void one(int xx, int y, int z, float cv)
 	{
-		if (y >= ny) return;
-		const bool rows_in = y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
-		const int cyz = cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
-		float* e = est + z * plane + y * pitch;
-		__nv_bfloat16* e16 = est16 + z * plane16 + y * pitch16;
-#pragma unroll
-		for (int h = 0; h < 2; ++h) {
-			const int xx = x + 32 * h;
-			if (xx >= nx) continue;
-			float s = s_interior;
-			if (!(rows_in && xx >= ilo[0] && xx <= ihi[0])) s = sens[cls[xx] + cyz];
-			const float cv = h ? c1 : c0;
-			const float factor = s > 0.0f ? cv / (s > eps ? s : eps) : 0.0f;
-			const float old = e[xx];
-			const float upd = old * factor;
-			e[xx] = upd;
-			e16[xx] = __float2bfloat16_rn(upd);
-			if (want_stats) {
-				kahan_add(f_s, f_c, upd);
-				const float d = upd - old;
-				kahan_add(c_s, c_c, d * d);
-				kahan_add(n_s, n_c, old * old);
-			}
-			if (write_out) {
-				char* q = out + xx * outs[0] + y * outs[1] + z * outs[2];
-				if (out_u8) {
-					*reinterpret_cast<uint8_t*>(q) = to_gray8(upd);
-				} else {
-					*reinterpret_cast<float*>(q) = upd;
-				}
+		if (y >= ny || xx >= nx) return;
+		const bool in = xx >= ilo[0] && xx <= ihi[0] && y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
+		const float s = in ? s_interior : sens[cls[xx] + cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z])];
+		const float factor = s > 0.0f ? cv / (s > eps ? s : eps) : 0.0f;
+		float* e = est + z * plane + y * pitch + xx;
+		const float old = *e;
+		const float upd = old * factor;
+		*e = upd;
+		est16[z * plane16 + y * pitch16 + xx] = __float2bfloat16_rn(upd);
+		if (want_stats) {
+			kahan_add(f_s, f_c, upd);
+			const float d = upd - old;
+			kahan_add(c_s, c_c, d * d);
+			kahan_add(n_s, n_c, old * old);
+		}
+		if (write_out) {
+			char* q = out + xx * outs[0] + y * outs[1] + z * outs[2];
+			if (out_u8) {
+				*reinterpret_cast<uint8_t*>(q) = to_gray8(upd);
+			} else {
+				*reinterpret_cast<float*>(q) = upd;
 			}
 		}
+	}
+
+	// one warp, one row: this lane's columns x and x + 32
+	__device__ __forceinline__ void row_pair(int x, int y, int z, float c0, float c1)
+	{
+		one(x, y, z, c0);
+		one(x + 32, y, z, c1);
+	}
+
+	// 16 consecutive outputs x0 .. x0 + 15 of row y (x0 a multiple of 16): vector loads and
+	// stores of the estimate and its BF16 shadow when the run lies inside the image
+	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&cv)[16])
+	{
+		if (y >= ny) return;
+		if (x0 + 16 > nx || write_out) {
+#pragma unroll
+			for (int c = 0; c < 16; ++c) one(x0 + c, y, z, cv[c]);
+			return;
+		}
+		const bool rows_in = y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
+		const bool all_in = rows_in && x0 >= ilo[0] && x0 + 15 <= ihi[0];
+		const int cyz = cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
+		float* e = est + z * plane + y * pitch + x0;  // rows are 16-byte aligned, x0 % 16 == 0
+		float old[16];
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			const float4 v = reinterpret_cast<const float4*>(e)[q];
+			old[4 * q] = v.x;
+			old[4 * q + 1] = v.y;
+			old[4 * q + 2] = v.z;
+			old[4 * q + 3] = v.w;
+		}
+		float upd[16];
+#pragma unroll
+		for (int c = 0; c < 16; ++c) {
+			float sv = s_interior;
+			if (!all_in && !(rows_in && x0 + c >= ilo[0] && x0 + c <= ihi[0])) sv = sens[cls[x0 + c] + cyz];
+			const float factor = sv > 0.0f ? cv[c] / (sv > eps ? sv : eps) : 0.0f;
+			upd[c] = old[c] * factor;
+			if (want_stats) {
+				kahan_add(f_s, f_c, upd[c]);
+				const float d = upd[c] - old[c];
+				kahan_add(c_s, c_c, d * d);
+				kahan_add(n_s, n_c, old[c] * old[c]);
+			}
+		}
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			reinterpret_cast<float4*>(e)[q] = make_float4(upd[4 * q], upd[4 * q + 1], upd[4 * q + 2], upd[4 * q + 3]);
+		}
+		uint32_t w[8];
+#pragma unroll
+		for (int c = 0; c < 8; ++c) {
+			const __nv_bfloat162 h = __floats2bfloat162_rn(upd[2 * c], upd[2 * c + 1]);
+			w[c] = *reinterpret_cast<const uint32_t*>(&h);
+		}
+		uint4* d16 = reinterpret_cast<uint4*>(est16 + z * plane16 + y * pitch16 + x0);
+		d16[0] = make_uint4(w[0], w[1], w[2], w[3]);
+		d16[1] = make_uint4(w[4], w[5], w[6], w[7]);
 	}
 
 	__device__ void finish()
@@ -283,5 +365,9 @@ struct EpiUpdateTc {
 
 int launch_tc_pass_a(const CUtensorMap& map, const TcArgs& a, const EpiRatioTc& e, cudaStream_t stream);
 int launch_tc_pass_b(const CUtensorMap& map, const TcArgs& a, const EpiUpdateTc& e, cudaStream_t stream);
+// The z-planes-along-N variant (rl_tcz.cuh): PSFs whose T matrices fit in shared memory.
+bool tcz_supported(int kx, int ky, int kz);
+int launch_tcz_pass_a(const CUtensorMap& map, const TcArgs& a, const EpiRatioTc& e, cudaStream_t stream);
+int launch_tcz_pass_b(const CUtensorMap& map, const TcArgs& a, const EpiUpdateTc& e, cudaStream_t stream);
 
 }  // namespace iane_gb

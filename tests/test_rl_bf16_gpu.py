@@ -28,7 +28,9 @@ def conv64(src, kernel):
     return out
 
 
-@pytest.mark.parametrize("shape,pshape", [((8, 72, 130), (9, 9, 9)), ((3, 140, 70), (3, 5, 7)), ((1, 40, 64), (1, 9, 17))])
+@pytest.mark.parametrize("shape,pshape", [((8, 72, 130), (9, 9, 9)), ((3, 140, 70), (3, 5, 7)), ((1, 40, 64), (1, 9, 17)),
+                                         ((13, 130, 50), (5, 7, 9)), ((20, 64, 48), (11, 11, 11)),
+                                         ((6, 40, 48), (15, 15, 15))])
 def test_one_iteration_matches_bf16_emulation(cuda, shape, pshape):
     rng = np.random.default_rng(sum(shape) + sum(pshape))
     psf = bf16(gaussian(pshape, [max(0.7, n / 4) for n in pshape]))
