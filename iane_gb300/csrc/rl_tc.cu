@@ -23,7 +23,7 @@ int launch_z(const CUtensorMap& map, const TcArgs& a, const Epi& e, cudaStream_t
 	IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes),
 		"tensor-core convolution: set shared memory size");
 	const dim3 grid((a.nx + 15) / 16, (a.ny + kTcM - 1) / kTcM, (a.nz + kTczZ - 1) / kTczZ);
-	kernel<<<grid, 128, a.smem_bytes, stream>>>(map, a, e);
+	kernel<<<grid, kTczThreads, a.smem_bytes, stream>>>(map, a, e);
 	IANE_GB_CUDA(cudaGetLastError(), "tensor-core convolution: launch");
 	return IANE_GB_OK;
 }

@@ -18,9 +18,12 @@
 //
 // TMEM holds ZC x 16 FP32 columns, zeroed with tcgen05.st first so that every MMA
 // accumulates. All T matrices (ky x 4 x kz KB) are loaded once per CTA by bulk copies; input
-// planes stream through three TMA stages (one elected thread issues loads and MMAs). The
-// epilogue reads each output plane's 16 columns and hands each thread's row of 16 voxels to
-// the pass epilogue (EpiRatioTc / EpiUpdateTc row16: vector loads and stores).
+// planes stream through three TMA stages. Warp specialised: one thread of warp 4 issues the
+// loads and MMAs and, once the last input plane reaching output plane i has been issued,
+// commits plane i to its own mbarrier; warps 0-3 (one TMEM lane = one output row each) finish
+// plane i meanwhile -- read its 16 columns and hand each thread's row of 16 voxels to the pass
+// epilogue (EpiRatioTc / EpiUpdateTc row16: vector loads and stores) -- so the epilogue of the
+// early planes overlaps the MMAs of the later ones.
 #pragma once
 
 #include "rl_tc.cuh"
@@ -35,8 +38,9 @@ inline __host__ __device__ size_t tcz_tmat_bytes(int ky, int kz) { return static
 inline __host__ __device__ size_t tcz_tile_bytes(int ky) { return static_cast<size_t>(kTczChunks) * tc_rows(ky) * 16; }
 inline size_t tcz_smem_bytes(int ky, int kz)
 {
-	return tcz_tmat_bytes(ky, kz) + kTczStages * tcz_tile_bytes(ky) + (2 * kTczStages + 3) * 8 + 16;
+	return tcz_tmat_bytes(ky, kz) + kTczStages * tcz_tile_bytes(ky) + (2 * kTczStages + 1 + kTczZ + 1) * 8 + 16;
 }
+constexpr int kTczThreads = 160; // warps 0-3: epilogue (TMEM lanes 0-127), warp 4: loads and MMAs
 
 __device__ __forceinline__ void tmem_st_zero16(uint32_t taddr)
 {
@@ -47,7 +51,7 @@ __device__ __forceinline__ void tmem_st_zero16(uint32_t taddr)
 }
 
 template<class Epi>
-__global__ void __launch_bounds__(128) tcz_conv_kernel(const __grid_constant__ CUtensorMap map, const TcArgs a,
+__global__ void __launch_bounds__(kTczThreads) tcz_conv_kernel(const __grid_constant__ CUtensorMap map, const TcArgs a,
 	const Epi epi_in)
 {
 	extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -72,31 +76,33 @@ __global__ void __launch_bounds__(128) tcz_conv_kernel(const __grid_constant__ C
 	uint64_t* full = bars;
 	uint64_t* empty = bars + kTczStages;
 	uint64_t* tmat_bar = bars + 2 * kTczStages;
-	uint64_t* done = tmat_bar + 1;
-	uint32_t& tmem_base_s = *reinterpret_cast<uint32_t*>(done + 1);
+	uint64_t* plane_bar = tmat_bar + 1;   // [kTczZ]: output plane i's accumulators are final
+	uint32_t& tmem_base_s = *reinterpret_cast<uint32_t*>(plane_bar + kTczZ);
 	constexpr uint32_t kCols = kTczZ * 16;
 
 	if (warp == 0) {
 		tc::tmem_alloc(&tmem_base_s, kCols);
 	}
 	if (tid == 0) {
-		for (int s = 0; s < 2 * kTczStages + 2; ++s) mbar_init(&bars[s], 1);
+		for (int s = 0; s < 2 * kTczStages + 1 + kTczZ; ++s) mbar_init(&bars[s], 1);
 		fence_barrier_init();
 	}
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
 	const uint32_t tmem = tmem_base_s;
-	// zero the accumulators: every MMA below accumulates
-	const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
+	// zero the accumulators (warps 0-3, one TMEM lane quarter each): every MMA accumulates
+	const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+	if (warp < 4) {
 #pragma unroll
-	for (int c = 0; c < static_cast<int>(kCols); c += 16) tmem_st_zero16(tmem + lane_base + c);
-	asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+		for (int c = 0; c < static_cast<int>(kCols); c += 16) tmem_st_zero16(tmem + lane_base + c);
+		asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+	}
 	tc::fence_before_sync();
 	__syncthreads();
 	tc::fence_after_sync();
 
-	if (tid == 0) {
+	if (tid == 128) {
 		bool ok = true;
 		// all T matrices, one bulk copy per kernel row
 		mbar_arrive_expect_tx(tmat_bar, tmat_bytes);
@@ -146,6 +152,10 @@ __global__ void __launch_bounds__(128) tcz_conv_kernel(const __grid_constant__ C
 				}
 			}
 			tc::commit(&empty[s]);
+			// output planes whose last input plane this was are final once these MMAs finish
+			for (int i = 0; i < nout; ++i) {
+				if (min(zin_hi, Z + i + rz) - zin_lo == p) tc::commit(&plane_bar[i]);
+			}
 			// the previous plane's stage is free once its MMAs finish: refill it
 			if (p >= 1 && p - 1 + kTczStages < np) {
 				const int sp = (p - 1) % kTczStages;
@@ -156,23 +166,22 @@ __global__ void __launch_bounds__(128) tcz_conv_kernel(const __grid_constant__ C
 				load(p - 1 + kTczStages);
 			}
 		}
-		tc::commit(done);
 	}
-	__syncwarp();
-	if (!mbar_wait_bounded(done, 0)) {
-		report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
-	}
-	__syncwarp();
-	tc::fence_after_sync();
-	// Epilogue, one output plane at a time: thread t holds row y0 + t's 16 consecutive
-	// columns and finishes them with 16-byte loads and stores (one memory round trip per
-	// plane for all 16 voxels).
+	// Epilogue (warps 0-3), one output plane at a time as its accumulators become final:
+	// thread t holds row y0 + t's 16 consecutive columns and finishes them with 16-byte loads
+	// and stores.
 	Epi epi = epi_in;
-	for (int i = 0; i < nout; ++i) {
-		float v[16];
-		__syncwarp();
-		tc::ld_32x32b_x16(tmem + lane_base + 16 * i, v);
-		epi.row16(x0, y0 + tid, Z + i, v);
+	if (warp < 4) {
+		for (int i = 0; i < nout; ++i) {
+			if (!mbar_wait_bounded(&plane_bar[i], 0)) {
+				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
+			}
+			__syncwarp(); // tcgen05.ld is warp-collective
+			tc::fence_after_sync();
+			float v[16];
+			tc::ld_32x32b_x16(tmem + lane_base + 16 * i, v);
+			epi.row16(x0, y0 + tid, Z + i, v);
+		}
 	}
 	tc::fence_before_sync();
 	__syncthreads();
