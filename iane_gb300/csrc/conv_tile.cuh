@@ -63,6 +63,10 @@ struct TileArgs {
 	int* status; // device status word for bounded waits
 };
 
+// Halo-tile and tap buffers: two (double buffering across kernel planes) for 3-D kernels,
+// one for single-plane kernels, which have nothing to double-buffer.
+__host__ __device__ inline int tile_buffers(int kz) { return kz > 1 ? 2 : 1; }
+
 // Shared memory bytes of one launch.
 template<int KX, int WX, int WY>
 inline size_t tile_smem_bytes(int ky, int kz)
@@ -70,8 +74,7 @@ inline size_t tile_smem_bytes(int ky, int kz)
 	const int H = 32 * WY + 2 * (ky / 2);
 	const size_t plane = (static_cast<size_t>(TileWidth<KX, WX>::P) * H * 4 + 127) & ~size_t(127);
 	const size_t psf = (static_cast<size_t>(ky) * TileGeom<KX>::KXP * 4 + 127) & ~size_t(127);
-	(void)kz;
-	return 2 * plane + 2 * psf + 16;
+	return tile_buffers(kz) * (plane + psf) + 16;
 }
 
 // One output tile (x0, y0, z) of the tiled convolution. Persistent kernels call it once per
@@ -96,7 +99,7 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 	const int H = TY + 2 * ry;
 	const int plane_floats = ((P * H + 31) & ~31);
 	float* tiles = reinterpret_cast<float*>(smem_raw);
-	float* psf_s = tiles + 2 * plane_floats; // taps of two kernel planes
+	float* psf_s = tiles + tile_buffers(kz) * plane_floats; // taps of one or two kernel planes
 	const int psf_floats = ((ky * G::KXP + 31) & ~31);
 
 	const int tid = threadIdx.x;
@@ -277,13 +280,14 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 
 // Shared memory bytes of the tile barriers (after the tiles and taps of conv_tile_body).
 template<int KX, int WX, int WY>
-__device__ __forceinline__ uint64_t* tile_barriers(int ky)
+__device__ __forceinline__ uint64_t* tile_barriers(int ky, int kz)
 {
 	extern __shared__ __align__(128) unsigned char smem_raw[];
 	const int H = 32 * WY + 2 * (ky / 2);
 	const int plane_floats = ((TileWidth<KX, WX>::P * H + 31) & ~31);
 	const int psf_floats = ((ky * TileGeom<KX>::KXP + 31) & ~31);
-	return reinterpret_cast<uint64_t*>(reinterpret_cast<float*>(smem_raw) + 2 * plane_floats + 2 * psf_floats);
+	return reinterpret_cast<uint64_t*>(reinterpret_cast<float*>(smem_raw) +
+		tile_buffers(kz) * (plane_floats + psf_floats));
 }
 
 template<int KX, int WX, int WY, bool TMA, class Epi>
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(32 * WX * WY)
 {
 	if constexpr (TMA) {
 		if (threadIdx.x == 0) {
-			uint64_t* bars = tile_barriers<KX, WX, WY>(a.ky);
+			uint64_t* bars = tile_barriers<KX, WX, WY>(a.ky, a.kz);
 			mbar_init(&bars[0], 1);
 			mbar_init(&bars[1], 1);
 			fence_barrier_init();
@@ -301,7 +305,7 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	Epi epi = epi_in;
 	uint32_t phases = 0;
 	conv_tile_body<KX, WX, WY, TMA, Epi>(&tmap, a, epi, blockIdx.x * 32 * WX, blockIdx.y * 32 * WY, blockIdx.z, phases,
-		tile_barriers<KX, WX, WY>(a.ky));
+		tile_barriers<KX, WX, WY>(a.ky, a.kz));
 	epi.finish();
 }
 

@@ -8,7 +8,7 @@ size_t batch_tile_smem(int wx, int kx, int ky)
 	const int H = 32 * wx + 2 * (ky / 2);
 	const size_t plane = (static_cast<size_t>(tile_pitch(kx, wx)) * H * 4 + 127) & ~size_t(127);
 	const size_t taps = (static_cast<size_t>(ky) * ((kx + 3) & ~3) * 4 + 127) & ~size_t(127);
-	return 2 * plane + 2 * taps + 16;
+	return plane + taps + 16; // 2-D images: one tile buffer and one tap buffer
 }
 
 const void* batch_kernel_handle(int wx)
