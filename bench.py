@@ -385,6 +385,46 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     return res
 
 
+def measure_fft_leg(dev, stream, reps=5):
+    """Spectral against direct convolution for large kernels: the 256x256x64 volume with
+    normalised 31x31x15 (sigma 4, 4, 2) and 31x31x31 (sigma 4) Gaussians, zero border; device
+    time per call (CUDA events), the largest difference relative to the direct result's
+    maximum, and which path `auto` picked."""
+    import torch
+
+    import iane_gb300
+    from iane_gb300 import synth
+
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(3)
+    vol = torch.rand((64, 256, 256), generator=gen, device=dev, dtype=torch.float32) * 1000
+    out = {}
+    for name, ext, sig in (("psf_31x31x15", (31, 31, 15), (4.0, 4.0, 2.0)), ("psf_31x31x31", (31, 31, 31), (4.0, 4.0, 4.0))):
+        psf = torch.from_numpy(synth.gaussian_psf(ext, sig)).to(dev)
+        leg, res = {}, {}
+        for method in ("direct", "fft", "auto"):
+            dst = torch.empty_like(vol)
+            run = lambda: iane_gb300.convolve(vol, psf, dst, "zero", method=method, stream=stream)
+            for _ in range(2):
+                run()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                run()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = a.elapsed_time(b) / reps
+            res[method] = dst.double()
+            leg[method] = {"ms": ms, "gvoxel_s": vol.numel() / (ms / 1e3) / 1e9}
+        leg["fft_vs_direct_max_rel"] = float((res["fft"] - res["direct"]).abs().max() / res["direct"].abs().max())
+        leg["speedup"] = leg["direct"]["ms"] / leg["fft"]["ms"]
+        leg["auto_picked"] = "fft" if torch.equal(res["auto"], res["fft"]) else "direct"
+        out[name] = leg
+    out["config"] = "256x256x64 f32, normalised Gaussian PSFs, zero border"
+    return out
+
+
 def measure_learned_leg(dev):
     """Learned warm start: the shipped network's start + BF16 tensor-core RL against plain FP32
     RL from the flat start on the 256x256x64 ellipsoid volume (200 ellipsoids), isotropic
@@ -495,6 +535,7 @@ def main():
     bf16_leg = measure_bf16_leg(dev, stream)
     batch_leg = measure_batch_leg(dev, stream, cpu=with_cpu)
     learned_leg = measure_learned_leg(dev)
+    fft_leg = measure_fft_leg(dev, stream)
 
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
@@ -554,6 +595,7 @@ def main():
             "bf16_tensor_leg": bf16_leg,
             "batch_leg": batch_leg,
             "learned_warm_start_leg": learned_leg,
+            "fft_leg": fft_leg,
         }
         print(json.dumps(line), flush=True)
     rl.close()

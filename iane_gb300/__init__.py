@@ -49,14 +49,19 @@ def _device_view(t) -> abi.View:
     return abi.torch_view(t)
 
 
-def convolve(src, kernel, dst, border="clamp", exact: bool = False, stream=None):
-    """Direct convolution of ``src`` with ``kernel`` into ``dst`` (all CUDA tensors).
+def convolve(src, kernel, dst, border="clamp", exact: bool = False, method: str = "direct", stream=None):
+    """Convolution of ``src`` with ``kernel`` into ``dst`` (all CUDA tensors).
 
     ``exact=True`` accumulates in FP64 in the reference's tap order, giving results
     bit-identical to the reference's CPU convolution; the default is FP32 accumulation
-    (int64 for integer image/kernel pairs). Asynchronous on ``stream``."""
+    (int64 for integer image/kernel pairs). ``method="fft"`` uses the spectral path (FP64
+    cuFFT transforms of the border-padded source; float types), ``method="auto"`` picks
+    direct or spectral by a cost model. Asynchronous on ``stream``."""
     s, k, d = _device_view(src), _device_view(kernel), _device_view(dst)
+    if method not in ("direct", "fft", "auto"):
+        raise ValueError(f"unknown method {method!r}")
     flags = abi.ACC_EXACT if exact else abi.ACC_FAST
+    flags |= {"direct": 0, "fft": abi.CONV_FFT, "auto": abi.CONV_AUTO}[method]
     check(lib().iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), _border(border), flags,
                                  _stream_handle(stream)))
     return dst

@@ -20,6 +20,7 @@ BORDER_CLAMP, BORDER_ZERO, BORDER_MIRROR = 0, 1, 2
 BORDERS = {"clamp": BORDER_CLAMP, "zero": BORDER_ZERO, "mirror": BORDER_MIRROR}
 
 ACC_FAST, ACC_EXACT = 0, 1
+CONV_FFT, CONV_AUTO = 2, 4
 
 RL_INIT_OBSERVED, RL_INIT_MEAN, RL_INIT_GIVEN = 0, 1, 2
 RL_BF16_TENSOR = 1

@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         objects = list(pool.map(lambda s: _compile(s, force, verbose), sources))
     if force or _stale(LIB, objects):
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objects]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objects] + ["-lcufft"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

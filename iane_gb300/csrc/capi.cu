@@ -253,8 +253,11 @@ int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const 
 	if (border < IANE_GB_BORDER_CLAMP || border > IANE_GB_BORDER_MIRROR) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "convolve: unknown border mode");
 	}
-	if (flags & ~IANE_GB_ACC_EXACT) {
+	if (flags & ~(IANE_GB_ACC_EXACT | IANE_GB_CONV_FFT | IANE_GB_CONV_AUTO)) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "convolve: unknown flags");
+	}
+	if ((flags & IANE_GB_ACC_EXACT) && (flags & (IANE_GB_CONV_FFT | IANE_GB_CONV_AUTO))) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "convolve: the exact mode has no spectral variant");
 	}
 	// convolution.hpp:107-113: positive odd kernel extents.
 	for (int i = 0; i < s.rank; ++i) {
@@ -279,6 +282,16 @@ int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const 
 	}
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	const bool exact = (flags & IANE_GB_ACC_EXACT) != 0;
+	if (flags & IANE_GB_CONV_FFT) {
+		return launch_conv_fft(s, k, d, border, st);
+	}
+	if ((flags & IANE_GB_CONV_AUTO) && conv_fft_supported(s, k, d)) {
+		double direct_s = 0.0, fft_s = 0.0;
+		conv_cost_model(s, k, direct_s, fft_s);
+		if (fft_s < direct_s) {
+			return launch_conv_fft(s, k, d, border, st);
+		}
+	}
 	if (!exact) {
 		status = launch_conv_f32_tiled(s, k, d, border, st);
 		if (status != IANE_GB_UNSUPPORTED) {

@@ -30,10 +30,9 @@ int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevVi
 	if (ky > 63 || src.ext[1] > 65535 * 32 || src.ext[2] > 65535) {
 		return IANE_GB_UNSUPPORTED;
 	}
-	// The kernel planes live in shared memory next to two halo tiles.
-	if (static_cast<long long>(kz) * ky * ((kx + 3) & ~3) * 4 > 96 * 1024) {
-		return IANE_GB_UNSUPPORTED;
-	}
+	// Shared memory holds one or two kernel planes' taps (ky x 32 floats at most) next to the
+	// halo tiles; the planes stream through it, so kz has no limit here.
+	(void)kz;
 	// TMA staging when the source is TMA-addressable (16-byte aligned rows and planes that do
 	// not overlap) and, for clamp and mirror, wider than the kernel radius on x and y (the
 	// edge fix-up takes its sources from inside the tile); else 4-byte cp.async staging.

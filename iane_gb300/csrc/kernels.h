@@ -13,6 +13,11 @@ int launch_conv_generic(const DevView& src, const DevView& kernel, const DevView
 // Register-tiled FP32 convolution (conv_f32.cu). Returns IANE_GB_UNSUPPORTED (without
 // recording an error) when the shapes are outside what the tiled path takes, so that the
 // caller falls back to the generic kernel.
+// Spectral convolution (conv_fft.cu): cuFFT FP64 transforms over the border-padded source.
+bool conv_fft_supported(const DevView& src, const DevView& kernel, const DevView& dst);
+void conv_cost_model(const DevView& src, const DevView& kernel, double& direct_s, double& fft_s);
+int launch_conv_fft(const DevView& src, const DevView& kernel, const DevView& dst, int border, cudaStream_t stream);
+
 int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevView& dst, int border,
 	cudaStream_t stream);
 

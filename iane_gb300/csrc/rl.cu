@@ -563,10 +563,9 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 	if (bf16 && k.ext[0] > 17) {
 		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: the BF16 tensor-core path takes PSFs up to 17 wide");
 	}
+	// The passes stream the PSF plane by plane through shared memory: kx <= 31 and ky <= 63
+	// (checked above) bound it, kz does not.
 	const long long taps = static_cast<long long>(k.ext[0]) * k.ext[1] * k.ext[2];
-	if (taps * ((k.ext[0] + 3) & ~3) / k.ext[0] * 4 > 96 * 1024) {
-		return fail(IANE_GB_UNSUPPORTED, "rl_prepare: PSF too large for shared memory");
-	}
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	auto* plan = new iane_gb_rl_plan{};
 	plan->rank = rank;

@@ -52,6 +52,18 @@ inline accumulation& thread_accumulation()
 	return mode;
 }
 
+/// Method for float convolution in fast accumulation: direct (tiled FP32), fft (cuFFT in
+/// FP64 over the border-padded source) or automatic (whichever a cost model predicts faster:
+/// the spectral path pays off for kernels of many thousands of taps).
+enum class method { direct, fft, automatic };
+
+/// Method used by iane::convolve on native views in the calling thread.
+inline method& thread_method()
+{
+	thread_local method m = method::direct;
+	return m;
+}
+
 namespace detail {
 
 template<class T> inline constexpr int dtype_code = 0;
@@ -203,7 +215,8 @@ namespace iane {
  *
  * Same contract as the reference's iane::convolve. Accumulation follows
  * iane::gb::thread_accumulation(): FP32 by default, FP64 in the reference's order when set
- * to accumulation::exact.
+ * to accumulation::exact. In fast accumulation, iane::gb::thread_method() selects the
+ * direct or the spectral (FFT) method for float views.
  */
 template<class TSrc, class TKernel, class TDst>
 requires (concepts::TransformViews<TSrc, TDst> &&
@@ -219,7 +232,10 @@ gb::execution convolve(TSrc aSource, TKernel aKernel, TDst aDestination,
 	const auto src = gb::detail::to_view(aSource);
 	const auto kernel = gb::detail::to_view(aKernel);
 	const auto dst = gb::detail::to_view(aDestination);
-	const unsigned flags = gb::thread_accumulation() == gb::accumulation::exact ? IANE_GB_ACC_EXACT : IANE_GB_ACC_FAST;
+	unsigned flags = gb::thread_accumulation() == gb::accumulation::exact ? IANE_GB_ACC_EXACT : IANE_GB_ACC_FAST;
+	if (flags == IANE_GB_ACC_FAST && gb::thread_method() != gb::method::direct) {
+		flags |= gb::thread_method() == gb::method::fft ? IANE_GB_CONV_FFT : IANE_GB_CONV_AUTO;
+	}
 	gb::detail::check(iane_gb_convolve(&src, &kernel, &dst, gb::detail::border_code(aOptions.border), flags,
 		aPolicy.stream));
 	return {{aPolicy.stream}};

@@ -67,6 +67,13 @@ typedef enum iane_gb_status {
 /* Convolution flags. */
 #define IANE_GB_ACC_FAST 0u  /* FP32 accumulation for float kernels, int64 for integer pairs */
 #define IANE_GB_ACC_EXACT 1u /* FP64 fma in kernel raster order: bit-identical to the reference */
+/* Spectral convolution (no counterpart in the reference's convolve; the reference has FFTs in
+ * include/iane/algorithms/fft/): f32/f64 source, kernel and destination; the border-padded
+ * source and the kernel are transformed with cuFFT in FP64, multiplied and transformed back,
+ * so results stay within the direct path's per-element bar while the work grows as
+ * L log L (L = padded size) instead of voxels x taps. */
+#define IANE_GB_CONV_FFT 2u  /* always the spectral path */
+#define IANE_GB_CONV_AUTO 4u /* direct FP32 or spectral, whichever a cost model predicts faster */
 
 typedef struct iane_gb_view {
 	void* ptr;              /* device address of element (0,...,0) */

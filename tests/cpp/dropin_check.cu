@@ -88,6 +88,19 @@ int main()
 		}
 	}
 	std::printf("ok   exact convolution matches the reference\n");
+	iane::gb::thread_accumulation() = iane::gb::accumulation::fast;
+	iane::gb::thread_method() = iane::gb::method::fft;
+	iane::convolve(d_src.const_view(), d_k.const_view(), d_out.view(), {iane::border_mode::zero}).wait();
+	iane::gb::thread_method() = iane::gb::method::direct;
+	iane::copy(d_out.const_view(), h_out.view()).wait();
+	for (int i = 0; i < 20 * 18 * 9; ++i) {
+		const float want = h_ref.pointer()[i];
+		if (std::fabs(h_out.pointer()[i] - want) > 1e-5f * (1.0f + std::fabs(want))) {
+			std::printf("FAIL FFT convolution differs at %d\n", i);
+			return 1;
+		}
+	}
+	std::printf("ok   FFT convolution matches the reference\n");
 	auto exec = iane::make_execution_context(iane::cuda_policy{});
 	auto op = exec.prepare(iane::gb::richardson_lucy{d_k.const_view(), 5, 1e-6f, iane::gb::rl_start::mean},
 		d_src.const_view(), d_out.view());

@@ -106,6 +106,8 @@ SHAPES = [
     ((19, 40, 72), (5, 3, 13)), ((2, 96, 100), (3, 11, 21)),
     # 16-byte aligned rows: TMA staging, clamp/mirror edges fixed up in shared memory
     ((9, 8), (15, 15)), ((16, 24), (13, 31)), ((5, 12, 20), (7, 9, 5)), ((3, 130, 260), (3, 7, 7)),
+    # 29791 taps on the tiled path (one kernel plane's taps in shared memory at a time)
+    ((20, 40, 36), (31, 31, 31)),
 ]
 
 
@@ -117,6 +119,12 @@ def test_random_f32_parity(cuda, shape, kshape, border):
     kernel = rng.standard_normal(kshape).astype(np.float32)
     ref = run_oracle(src, kernel, np.float32, border)
     check_fp32(run_gpu(src, kernel, np.float32, border), ref, src, kernel, border)
+    if kernel.size * 8 > 200 * 1024:
+        # the exact (FP64) mode keeps all taps in shared memory and refuses larger kernels
+        with pytest.raises(iane_gb300.IaneError) as err:
+            run_gpu(src, kernel, np.float32, border, exact=True)
+        assert err.value.status == iane_gb300.abi.UNSUPPORTED
+        return
     assert np.array_equal(run_gpu(src, kernel, np.float32, border, exact=True), ref)
 
 
@@ -234,3 +242,78 @@ def test_errors_raise_before_launch(cuda):
     empty = to_gpu(np.zeros((0, 8), np.float32))
     iane_gb300.convolve(empty, to_gpu(np.ones((3, 3), np.float32)), empty.clone())
     iane_gb300.device_status()
+
+
+# --- spectral (FFT) convolution ---------------------------------------------------------
+
+@pytest.mark.parametrize("border", ["clamp", "zero", "mirror"])
+@pytest.mark.parametrize("shape,kshape", [((300,), (61,)), ((40, 70), (31, 21)), ((12, 30, 50), (9, 15, 21)),
+                                          ((3, 5, 4), (7, 9, 11)), ((1, 33, 17), (1, 5, 3))])
+def test_fft_convolution_parity(cuda, shape, kshape, border):
+    """The spectral path against the FP64 oracle, with the direct FP32 path's per-element bar."""
+    rng = np.random.default_rng(zlib.crc32(repr(("fft", shape, kshape, border)).encode()))
+    src = rng.standard_normal(shape).astype(np.float32)
+    kernel = rng.standard_normal(kshape).astype(np.float32)
+    ref = run_oracle(src, kernel, np.float32, border)
+    d = empty_like_np(shape, np.float32)
+    iane_gb300.convolve(to_gpu(src), to_gpu(kernel), d, border, method="fft")
+    check_fp32(to_host(d), ref, src, kernel, border)
+    # f64 destination: FP64 transforms, far inside the bar
+    d64 = empty_like_np(shape, np.float64)
+    iane_gb300.convolve(to_gpu(src), to_gpu(kernel), d64, border, method="fft")
+    ref64 = run_oracle(src, kernel, np.float64, border)
+    assert rel_err_bound(to_host(d64), ref64, magnitude(src, kernel, border)) <= 1e-9
+
+
+def test_fft_strided_and_cropped_views(cuda):
+    """Strided source and destination crops go through the pad and crop kernels' view
+    addressing; the padding around the destination crop stays untouched."""
+    t = torch()
+    rng = np.random.default_rng(31)
+    big = rng.random((11, 40, 50), dtype=np.float32)
+    kernel = rng.random((5, 9, 7), dtype=np.float32)
+    src_np = big[2:9, 3:37:2, 5:46]
+    g = to_gpu(big)[2:9, 3:37:2, 5:46]
+    dst_big = t.zeros((9, 20, 90), device="cuda")
+    dst = dst_big[1:8, 1:18, 3:85:2][:, :, : src_np.shape[2]]
+    for border in ("clamp", "zero", "mirror"):
+        ref = run_oracle(np.ascontiguousarray(src_np), kernel, np.float32, border)
+        iane_gb300.convolve(g, to_gpu(kernel), dst, border, method="fft")
+        check_fp32(to_host(dst), ref, src_np, kernel, border)
+    mask = t.ones_like(dst_big, dtype=t.bool)
+    mask[1:8, 1:18, 3:85:2] = False
+    assert float(dst_big[mask].abs().max()) == 0.0
+
+
+def test_fft_auto_picks_one_of_the_two_paths(cuda):
+    """`auto` returns bit-for-bit the direct or the spectral result; for a 31^3 kernel on a
+    64x128x128 volume the cost model picks the spectral path."""
+    rng = np.random.default_rng(21)
+    src = to_gpu(rng.random((64, 128, 128), dtype=np.float32))
+    kernel = to_gpu((rng.random((31, 31, 31), dtype=np.float32) / 31 ** 3).astype(np.float32))
+    outs = {}
+    for method in ("direct", "fft", "auto"):
+        d = empty_like_np((64, 128, 128), np.float32)
+        iane_gb300.convolve(src, kernel, d, "zero", method=method)
+        outs[method] = to_host(d)
+    assert np.array_equal(outs["auto"], outs["fft"])
+    # the direct path sums 29791 taps in FP32 (about 1e-5 of the maximum); the spectral one
+    # carries FP64 transforms, so the difference is the direct path's rounding
+    assert float(np.max(np.abs(outs["fft"] - outs["direct"]) / np.abs(outs["direct"]).max())) < 3e-5
+    small = to_gpu(rng.random((3, 3, 3), dtype=np.float32))
+    d1, d2 = empty_like_np((64, 128, 128), np.float32), empty_like_np((64, 128, 128), np.float32)
+    iane_gb300.convolve(src, small, d1, "zero", method="auto")
+    iane_gb300.convolve(src, small, d2, "zero", method="direct")
+    assert np.array_equal(to_host(d1), to_host(d2))
+
+
+def test_fft_rejects_integer_types_and_exact_mode(cuda):
+    a = to_gpu(np.zeros((16, 16), np.uint8))
+    k = to_gpu(np.ones((3, 3), np.int32))
+    with pytest.raises(iane_gb300.IaneError) as info:
+        iane_gb300.convolve(a, k, a.clone(), "zero", method="fft")
+    assert info.value.status == iane_gb300.abi.UNSUPPORTED
+    f = to_gpu(np.zeros((16, 16), np.float32))
+    kf = to_gpu(np.ones((3, 3), np.float32))
+    with pytest.raises(iane_gb300.IaneInvalidArgument):
+        iane_gb300.convolve(f, kf, f.clone(), "zero", exact=True, method="fft")

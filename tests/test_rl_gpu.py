@@ -55,6 +55,8 @@ CASES = [
     ((61,), (9,), 0), ((40, 53), (7, 5), 1), ((33, 47), (31, 3), 0), ((5, 6), (9, 11), 1),
     ((12, 40, 44), (5, 7, 9), 1), ((16, 64, 72), (7, 15, 15), 1), ((9, 17, 23), (3, 5, 29), 0),
     ((3, 4, 5), (5, 9, 7), 1),
+    # a 29791-tap PSF: planes stream through shared memory, kz unbounded
+    ((12, 40, 36), (31, 31, 31), 1),
 ]
 
 
