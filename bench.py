@@ -425,6 +425,68 @@ def measure_fft_leg(dev, stream, reps=5):
     return out
 
 
+def measure_reference_benchmark_leg(dev, stream, cpu=True, reps=20):
+    """The reference's own convolution benchmark (benchmarks/convolution.cu:84-118): a
+    2560x1920 u8 image ((i * 19) ^ (i / width)), a 9x9 f32 kernel (((i * 3) % 7 - 2) / 64),
+    clamp border, from a linear device image and from a texture. Device time per call (CUDA
+    events), and whether the output is byte-identical to the reference's serial CPU result
+    (SHA-256 kept with the golden vectors). The CPU baseline is the oracle port on all host
+    threads and on one (the reference times serial, 4 and 8 workers)."""
+    import hashlib
+
+    import numpy as np
+    import torch
+
+    import iane_gb300
+
+    width, height = 2560, 1920
+    i = np.arange(width * height, dtype=np.int64)
+    image = (((i * 19) ^ (i // width)) & 0xFF).astype(np.uint8).reshape(height, width)
+    k = np.arange(81, dtype=np.int64)
+    kernel = (((k * 3) % 7 - 2) / 64.0).astype(np.float32).reshape(9, 9)
+    golden = np.load(Path(__file__).resolve().parent / "tests" / "golden" / "golden.npz")
+    want = str(golden["bench_u8_2560x1920__sha256"])
+    src = torch.from_numpy(image).to(dev)
+    kd = torch.from_numpy(kernel).to(dev)
+    dst = torch.empty_like(src)
+    tex = iane_gb300.Texture(image.shape, "uint8").upload(src, stream=stream)
+    out = {}
+    for name, source, exact in (("linear", src, False), ("texture", tex.view(), False), ("linear_exact_fp64", src, True)):
+        run = lambda: iane_gb300.convolve(source, kd, dst, "clamp", exact=exact, stream=stream)
+        for _ in range(3):
+            run()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            run()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = a.elapsed_time(b) / reps
+        digest = hashlib.sha256(dst.cpu().numpy().tobytes()).hexdigest()
+        out[name] = {"ms": ms, "gpixel_s": image.size / (ms / 1e3) / 1e9,
+                     "tflops": 2 * 81 * image.size / (ms / 1e3) / 1e12, "bit_exact_vs_reference": digest == want}
+    tex.close()
+    if cpu:
+        import oracle
+        from oracle import build as oracle_build
+
+        oracle_build.build_oracle()
+        ref_np = np.zeros_like(image)
+        for threads in (oracle.default_threads(), 1):
+            t0 = time.perf_counter()
+            n = 0
+            while n == 0 or time.perf_counter() - t0 < 1.0:
+                oracle.convolve(image, kernel, ref_np, "clamp", threads=threads)
+                n += 1
+            cms = (time.perf_counter() - t0) / n * 1e3
+            key = "cpu_baseline_all_threads" if threads > 1 else "cpu_baseline_1_thread"
+            out[key] = {"ms": cms, "cores": threads, "kind": "port", "sample": f"{n} full image(s)"}
+        out["gpu_speedup_vs_all_threads"] = out["cpu_baseline_all_threads"]["ms"] / out["linear"]["ms"]
+    out["config"] = "2560x1920 u8, 9x9 f32 kernel (k/64), clamp"
+    return out
+
+
 def measure_learned_leg(dev):
     """Learned warm start: the shipped network's start + BF16 tensor-core RL against plain FP32
     RL from the flat start on the 256x256x64 ellipsoid volume (200 ellipsoids), isotropic
@@ -536,6 +598,7 @@ def main():
     batch_leg = measure_batch_leg(dev, stream, cpu=with_cpu)
     learned_leg = measure_learned_leg(dev)
     fft_leg = measure_fft_leg(dev, stream)
+    reference_benchmark_leg = measure_reference_benchmark_leg(dev, stream, cpu=with_cpu)
 
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
@@ -596,6 +659,7 @@ def main():
             "batch_leg": batch_leg,
             "learned_warm_start_leg": learned_leg,
             "fft_leg": fft_leg,
+            "reference_benchmark_leg": reference_benchmark_leg,
         }
         print(json.dumps(line), flush=True)
     rl.close()

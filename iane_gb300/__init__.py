@@ -7,6 +7,12 @@ supplies device memory and streams only; every computation runs in ``libiane_gb3
   (reference include/iane/algorithms/convolution.hpp:97-117): odd kernel extents, the
   kernel flipped, same extents in and out, reference casts for integer outputs.
 * :func:`convolve_separable` -- the same with an outer-product kernel, one fused pass.
+* :func:`convolve_rgb8` -- packed (r, g, b) byte pixels, each channel summed on its own: the
+  custom element of the reference's convolution example (examples/convolution/main.cu:20-56).
+* :class:`Texture` / :class:`TextureView` -- the reference's texture_image and
+  texture_image_view (include/iane/resource/cuda/texture_image.hpp,
+  include/iane/view/texture_image_view.hpp); a :class:`TextureView` is a valid ``src`` of
+  :func:`convolve`.
 * :class:`RichardsonLucy` -- the prepared-algorithm protocol of
   include/iane/execution/prepared.hpp:120-146 (``prepare`` sizes the scratch, ``run``
   consumes it) applied to the RL loop of examples/rl_deconvolution/main.cu:51-81.
@@ -22,8 +28,8 @@ from . import abi
 from ._lib import IaneError, IaneInvalidArgument, IaneLengthError, check, lib
 
 __all__ = [
-    "abi", "convolve", "convolve_separable", "RichardsonLucy", "RichardsonLucyBatch", "device_status", "IaneError",
-    "IaneInvalidArgument", "IaneLengthError",
+    "abi", "convolve", "convolve_separable", "convolve_rgb8", "Texture", "TextureView", "RichardsonLucy",
+    "RichardsonLucyBatch", "device_status", "IaneError", "IaneInvalidArgument", "IaneLengthError",
 ]
 
 
@@ -57,14 +63,108 @@ def convolve(src, kernel, dst, border="clamp", exact: bool = False, method: str 
     (int64 for integer image/kernel pairs). ``method="fft"`` uses the spectral path (FP64
     cuFFT transforms of the border-padded source; float types), ``method="auto"`` picks
     direct or spectral by a cost model. Asynchronous on ``stream``."""
-    s, k, d = _device_view(src), _device_view(kernel), _device_view(dst)
     if method not in ("direct", "fft", "auto"):
         raise ValueError(f"unknown method {method!r}")
     flags = abi.ACC_EXACT if exact else abi.ACC_FAST
     flags |= {"direct": 0, "fft": abi.CONV_FFT, "auto": abi.CONV_AUTO}[method]
+    k, d = _device_view(kernel), _device_view(dst)
+    if isinstance(src, TextureView):
+        tv = src._abi()
+        check(lib().iane_gb_convolve_texture(ctypes.byref(tv), ctypes.byref(k), ctypes.byref(d), _border(border),
+                                             flags, _stream_handle(stream)))
+        return dst
+    s = _device_view(src)
     check(lib().iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), _border(border), flags,
                                  _stream_handle(stream)))
     return dst
+
+
+def _rgb8_device_view(t) -> abi.View:
+    if not t.is_cuda or str(t.dtype) != "torch.uint8":
+        raise ValueError("an rgb8 image is a CUDA uint8 tensor of shape (..., 3)")
+    return abi.rgb8_view(t.data_ptr(), tuple(t.shape), tuple(t.stride()))
+
+
+def convolve_rgb8(src, kernel, dst, border="clamp", exact: bool = False, stream=None):
+    """Convolution of packed rgb8 pixels: ``src`` and ``dst`` are uint8 CUDA tensors of shape
+    ``(..., 3)`` (channels contiguous), ``kernel`` an f32 tensor of the image rank. Each
+    channel is convolved on its own and converted with the byte rule; ``exact=True`` gives the
+    reference's per-channel double sums bit for bit."""
+    s, d, k = _rgb8_device_view(src), _rgb8_device_view(dst), _device_view(kernel)
+    flags = abi.ACC_EXACT if exact else abi.ACC_FAST
+    check(lib().iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), _border(border), flags,
+                                 _stream_handle(stream)))
+    return dst
+
+
+class Texture:
+    """A CUDA array with its point-sampled texture object (the reference's texture_image).
+
+    ``shape`` is C-ordered like tensors; ``dtype`` a torch or numpy dtype name of a texel type
+    (u8, i8, u16, i16, i32, u32, f32). ``upload`` copies a host (numpy) or CUDA (torch) array of
+    that shape and type; ``view()`` borrows the whole texture as a convolution source."""
+
+    def __init__(self, shape, dtype):
+        code = abi._TORCH_DTYPES.get(str(dtype), abi._NUMPY_DTYPES.get(str(dtype)))
+        if code not in abi.TEXEL_DTYPES:
+            raise TypeError(f"texture element type {dtype} is not one of u8, i8, u16, i16, i32, u32, f32")
+        self.shape = tuple(int(n) for n in shape)
+        self.dtype = code
+        rank = len(self.shape)
+        ext = (ctypes.c_int32 * 3)(*([self.shape[rank - 1 - i] for i in range(rank)] + [1] * (3 - rank)))
+        handle = ctypes.c_uint64(0)
+        check(lib().iane_gb_texture_create(code, rank, ext, ctypes.byref(handle)))
+        self.handle = handle.value
+
+    def upload(self, array, stream=None) -> "Texture":
+        if hasattr(array, "is_cuda"):
+            v = abi.torch_view(array)
+        else:
+            v = abi.numpy_view(array)
+        check(lib().iane_gb_texture_upload(self.handle, ctypes.byref(v), _stream_handle(stream)))
+        return self
+
+    def view(self) -> "TextureView":
+        return TextureView(self, (0,) * len(self.shape), self.shape)
+
+    def close(self) -> None:
+        if getattr(self, "handle", 0):
+            check(lib().iane_gb_texture_destroy(self.handle))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TextureView:
+    """A region of a :class:`Texture` (texture_image_view): ``origin`` and ``shape`` C-ordered."""
+
+    def __init__(self, texture: Texture, origin, shape):
+        if len(origin) != len(texture.shape) or len(shape) != len(texture.shape):
+            raise ValueError("origin and shape need the texture's rank")
+        self.texture = texture
+        self.origin = tuple(int(o) for o in origin)
+        self.shape = tuple(int(n) for n in shape)
+
+    def subview(self, origin, shape) -> "TextureView":
+        """An in-bounds region whose coordinates start at zero (texture_image_view::subview)."""
+        if any(o < 0 or n < 0 or o + n > m for o, n, m in zip(origin, shape, self.shape)):
+            raise ValueError("subview outside the view")
+        return TextureView(self.texture, tuple(a + b for a, b in zip(self.origin, origin)), shape)
+
+    def _abi(self) -> abi.TextureView:
+        rank = len(self.shape)
+        tv = abi.TextureView()
+        tv.texture = self.texture.handle
+        tv.dtype = self.texture.dtype
+        tv.rank = rank
+        for i in range(3):
+            tv.extent[i] = self.shape[rank - 1 - i] if i < rank else 1
+            tv.origin[i] = self.origin[rank - 1 - i] if i < rank else 0
+        return tv
 
 
 def convolve_separable(src, taps, dst, border="clamp", stream=None):

@@ -107,6 +107,13 @@ def lib() -> ctypes.CDLL:
         getattr(l, "iane_gb_cnn_" + name).restype = ctypes.c_int
     l.iane_gb_rl_destroy.argtypes = [vp]
     l.iane_gb_rl_destroy.restype = ctypes.c_int
+    u64 = ctypes.c_uint64
+    l.iane_gb_texture_create.argtypes = [i, i, i32p, ctypes.POINTER(u64)]
+    l.iane_gb_texture_upload.argtypes = [u64, _VIEW_P, vp]
+    l.iane_gb_texture_destroy.argtypes = [u64]
+    l.iane_gb_convolve_texture.argtypes = [ctypes.POINTER(abi.TextureView), _VIEW_P, _VIEW_P, i, ctypes.c_uint, vp]
+    for name in ("texture_create", "texture_upload", "texture_destroy", "convolve_texture"):
+        getattr(l, "iane_gb_" + name).restype = ctypes.c_int
     if l.iane_gb_abi_version() != abi.ABI_VERSION:
         raise RuntimeError("libiane_gb300.so ABI version mismatch; rebuild it")
     _lib = l

@@ -13,8 +13,9 @@ import ctypes
 ABI_VERSION = 1
 MAX_RANK = 3
 
-U8, U16, I16, I32, F32, F64, BF16 = 1, 2, 3, 4, 5, 6, 7
-DTYPE_SIZE = {U8: 1, U16: 2, I16: 2, I32: 4, F32: 4, F64: 8, BF16: 2}
+U8, U16, I16, I32, F32, F64, BF16, I8, U32, RGB8 = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
+DTYPE_SIZE = {U8: 1, U16: 2, I16: 2, I32: 4, F32: 4, F64: 8, BF16: 2, I8: 1, U32: 4, RGB8: 3}
+TEXEL_DTYPES = (U8, I8, U16, I16, I32, U32, F32)
 
 BORDER_CLAMP, BORDER_ZERO, BORDER_MIRROR = 0, 1, 2
 BORDERS = {"clamp": BORDER_CLAMP, "zero": BORDER_ZERO, "mirror": BORDER_MIRROR}
@@ -45,10 +46,12 @@ STATUS_NAMES = {
 
 _NUMPY_DTYPES = {
     "uint8": U8, "uint16": U16, "int16": I16, "int32": I32, "float32": F32, "float64": F64,
+    "int8": I8, "uint32": U32,
 }
 _TORCH_DTYPES = {
     "torch.uint8": U8, "torch.uint16": U16, "torch.int16": I16, "torch.int32": I32,
-    "torch.float32": F32, "torch.float64": F64, "torch.bfloat16": BF16,
+    "torch.float32": F32, "torch.float64": F64, "torch.bfloat16": BF16, "torch.int8": I8,
+    "torch.uint32": U32,
 }
 
 
@@ -60,6 +63,16 @@ class View(ctypes.Structure):
         ("extent", ctypes.c_int32 * 3),
         ("reserved", ctypes.c_int32),
         ("stride", ctypes.c_int64 * 3),
+    ]
+
+
+class TextureView(ctypes.Structure):
+    _fields_ = [
+        ("texture", ctypes.c_uint64),
+        ("dtype", ctypes.c_int32),
+        ("rank", ctypes.c_int32),
+        ("extent", ctypes.c_int32 * 3),
+        ("origin", ctypes.c_int32 * 3),
     ]
 
 
@@ -84,6 +97,14 @@ def numpy_view(arr) -> View:
     if code is None:
         raise TypeError(f"unsupported numpy dtype {arr.dtype}")
     return make_view(arr.ctypes.data, code, arr.shape, arr.strides)
+
+
+def rgb8_view(ptr: int, shape, strides_bytes) -> View:
+    """View of packed (r, g, b) pixels held as a uint8 array of shape (..., 3) whose last
+    axis is contiguous; ``shape``/``strides_bytes`` are the array's, channel axis included."""
+    if len(shape) < 2 or shape[-1] != 3 or strides_bytes[-1] != 1:
+        raise ValueError("an rgb8 image is a uint8 array of shape (..., 3) with contiguous channels")
+    return make_view(ptr, RGB8, tuple(shape[:-1]), tuple(strides_bytes[:-1]))
 
 
 def torch_view(t) -> View:

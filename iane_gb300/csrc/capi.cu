@@ -37,6 +37,9 @@ int dtype_size(int dtype)
 	case IANE_GB_F32: return 4;
 	case IANE_GB_F64: return 8;
 	case IANE_GB_BF16: return 2;
+	case IANE_GB_I8: return 1;
+	case IANE_GB_U32: return 4;
+	case IANE_GB_RGB8: return 3;
 	default: return 0;
 	}
 }
@@ -51,6 +54,9 @@ const char* dtype_name(int dtype)
 	case IANE_GB_F32: return "f32";
 	case IANE_GB_F64: return "f64";
 	case IANE_GB_BF16: return "bf16";
+	case IANE_GB_I8: return "i8";
+	case IANE_GB_U32: return "u32";
+	case IANE_GB_RGB8: return "rgb8";
 	default: return "?";
 	}
 }
@@ -87,7 +93,7 @@ int normalise_view(const iane_gb_view* view, const char* name, DevView* out)
 	if (count > 0 && !v.ptr) {
 		return fail(IANE_GB_INVALID_ARGUMENT, std::string(name) + ": null pointer for a nonempty view");
 	}
-	const int size = dtype_size(v.dtype);
+	const int size = v.dtype == IANE_GB_RGB8 ? 1 : dtype_size(v.dtype); // alignment: a packed pixel has 1
 	if (count > 0 && (reinterpret_cast<uintptr_t>(v.ptr) % size) != 0) {
 		return fail(IANE_GB_INVALID_ARGUMENT, std::string(name) + ": pointer not aligned to its element");
 	}
@@ -237,16 +243,13 @@ int iane_gb_device_status(void* stream)
 	return IANE_GB_OK;
 }
 
-int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const iane_gb_view* dst, int border,
-	unsigned flags, void* stream)
+}  // extern "C"
+
+namespace iane_gb {
+
+int convolve_checked(const DevView& s, const DevView& k, const DevView& d, int border, unsigned flags, void* stream,
+	const TexSource* tex)
 {
-	DevView s{}, k{}, d{};
-	int status = normalise_view(src, "convolve source", &s);
-	if (status) return status;
-	status = normalise_view(kernel, "convolve kernel", &k);
-	if (status) return status;
-	status = normalise_view(dst, "convolve destination", &d);
-	if (status) return status;
 	if (s.rank != k.rank || s.rank != d.rank) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "convolve: source, kernel and destination need the same rank");
 	}
@@ -277,11 +280,38 @@ int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const 
 	if (d.dtype == IANE_GB_BF16) {
 		return fail(IANE_GB_UNSUPPORTED, "convolve: bf16 destinations are not supported");
 	}
+	const bool rgb = s.dtype == IANE_GB_RGB8 || d.dtype == IANE_GB_RGB8;
+	if (rgb && (s.dtype != d.dtype || k.dtype != IANE_GB_F32 || tex)) {
+		return fail(IANE_GB_UNSUPPORTED, "convolve: rgb8 takes an rgb8 source and destination and an f32 kernel");
+	}
+	if (tex && (flags & (IANE_GB_CONV_FFT | IANE_GB_CONV_AUTO))) {
+		return fail(IANE_GB_UNSUPPORTED, "convolve: texture sources have no spectral path");
+	}
 	if (element_count(s) == 0) {
 		return IANE_GB_OK;
 	}
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	const bool exact = (flags & IANE_GB_ACC_EXACT) != 0;
+	if (rgb) {
+		if (flags & IANE_GB_CONV_FFT) {
+			return fail(IANE_GB_UNSUPPORTED, "convolve: rgb8 has no spectral path");
+		}
+		// Each channel is a u8 image at byte offset c with the pixel strides. A pixel's sum is
+		// per channel: (pixel * k) adds r, g and b independently, and each channel's product
+		// of a byte and an f32 tap is exact in FP64, so the reference's sum + product equals
+		// the exact mode's fma and the byte conversion is the u8 rule.
+		for (int c = 0; c < 3; ++c) {
+			DevView sc = s, dc = d;
+			sc.dtype = dc.dtype = IANE_GB_U8;
+			sc.ptr += c;
+			dc.ptr += c;
+			int status = IANE_GB_UNSUPPORTED;
+			if (!exact) status = launch_conv_f32_tiled(sc, k, dc, border, st);
+			if (status == IANE_GB_UNSUPPORTED) status = launch_conv_generic(sc, k, dc, border, exact, st);
+			if (status) return status;
+		}
+		return IANE_GB_OK;
+	}
 	if (flags & IANE_GB_CONV_FFT) {
 		return launch_conv_fft(s, k, d, border, st);
 	}
@@ -293,12 +323,29 @@ int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const 
 		}
 	}
 	if (!exact) {
-		status = launch_conv_f32_tiled(s, k, d, border, st);
+		const int status = launch_conv_f32_tiled(s, k, d, border, st, tex);
 		if (status != IANE_GB_UNSUPPORTED) {
 			return status;
 		}
 	}
-	return launch_conv_generic(s, k, d, border, exact, st);
+	return launch_conv_generic(s, k, d, border, exact, st, tex);
+}
+
+}  // namespace iane_gb
+
+extern "C" {
+
+int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const iane_gb_view* dst, int border,
+	unsigned flags, void* stream)
+{
+	DevView s{}, k{}, d{};
+	int status = normalise_view(src, "convolve source", &s);
+	if (status) return status;
+	status = normalise_view(kernel, "convolve kernel", &k);
+	if (status) return status;
+	status = normalise_view(dst, "convolve destination", &d);
+	if (status) return status;
+	return convolve_checked(s, k, d, border, flags, stream, nullptr);
 }
 
 int iane_gb_convolve_separable(const iane_gb_view* src, const iane_gb_view* const* taps, const iane_gb_view* dst,

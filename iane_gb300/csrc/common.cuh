@@ -70,6 +70,8 @@ template<> struct dtype_of<int32_t> { static constexpr int value = IANE_GB_I32; 
 template<> struct dtype_of<float> { static constexpr int value = IANE_GB_F32; };
 template<> struct dtype_of<double> { static constexpr int value = IANE_GB_F64; };
 template<> struct dtype_of<__nv_bfloat16> { static constexpr int value = IANE_GB_BF16; };
+template<> struct dtype_of<int8_t> { static constexpr int value = IANE_GB_I8; };
+template<> struct dtype_of<uint32_t> { static constexpr int value = IANE_GB_U32; };
 
 template<class T> __device__ __forceinline__ float to_float(T v) { return static_cast<float>(v); }
 template<> __device__ __forceinline__ float to_float<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
@@ -109,8 +111,81 @@ template<> __device__ __forceinline__ int32_t convert_sum<int32_t>(double sum)
 {
 	return saturate_integral<int32_t>(sum, -2147483648.0, 2147483647.0, INT32_MIN, INT32_MAX);
 }
+template<> __device__ __forceinline__ int8_t convert_sum<int8_t>(double sum)
+{
+	return saturate_integral<int8_t>(sum, -128.0, 127.0, -128, 127);
+}
+template<> __device__ __forceinline__ uint32_t convert_sum<uint32_t>(double sum)
+{
+	return saturate_integral<uint32_t>(sum, 0.0, 4294967295.0, 0u, 4294967295u);
+}
 template<> __device__ __forceinline__ float convert_sum<float>(double sum) { return static_cast<float>(sum); }
 template<> __device__ __forceinline__ double convert_sum<double>(double sum) { return sum; }
+
+// One element of a runtime element type as float (u8..u32, bf16 and f32 are exact for the
+// 8- and 16-bit types; i32/u32 round as a float conversion does).
+__device__ __forceinline__ float load_as_float(const char* p, int dtype)
+{
+	switch (dtype) {
+	case IANE_GB_U8: return static_cast<float>(*reinterpret_cast<const uint8_t*>(p));
+	case IANE_GB_I8: return static_cast<float>(*reinterpret_cast<const int8_t*>(p));
+	case IANE_GB_U16: return static_cast<float>(*reinterpret_cast<const uint16_t*>(p));
+	case IANE_GB_I16: return static_cast<float>(*reinterpret_cast<const int16_t*>(p));
+	case IANE_GB_I32: return static_cast<float>(*reinterpret_cast<const int32_t*>(p));
+	case IANE_GB_U32: return static_cast<float>(*reinterpret_cast<const uint32_t*>(p));
+	case IANE_GB_BF16: return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(p));
+	case IANE_GB_F32: return *reinterpret_cast<const float*>(p);
+	default: return 0.0f;
+	}
+}
+
+// Store a sum into a runtime destination element type with the reference's conversion.
+__device__ __forceinline__ void store_converted(char* p, int dtype, double sum)
+{
+	switch (dtype) {
+	case IANE_GB_U8: *reinterpret_cast<uint8_t*>(p) = convert_sum<uint8_t>(sum); break;
+	case IANE_GB_I8: *reinterpret_cast<int8_t*>(p) = convert_sum<int8_t>(sum); break;
+	case IANE_GB_U16: *reinterpret_cast<uint16_t*>(p) = convert_sum<uint16_t>(sum); break;
+	case IANE_GB_I16: *reinterpret_cast<int16_t*>(p) = convert_sum<int16_t>(sum); break;
+	case IANE_GB_I32: *reinterpret_cast<int32_t*>(p) = convert_sum<int32_t>(sum); break;
+	case IANE_GB_U32: *reinterpret_cast<uint32_t*>(p) = convert_sum<uint32_t>(sum); break;
+	case IANE_GB_F32: *reinterpret_cast<float*>(p) = convert_sum<float>(sum); break;
+	case IANE_GB_F64: *reinterpret_cast<double*>(p) = sum; break;
+	default: break;
+	}
+}
+
+// A texel of a point-sampled texture with unnormalised coordinates, read at its centre as
+// the reference's texture_image_view::operator[] does (texture_image_view.hpp:45-53).
+template<class T>
+__device__ __forceinline__ T texel(cudaTextureObject_t tex, int rank, int x, int y, int z)
+{
+	if (rank == 1) return tex1D<T>(tex, x + 0.5f);
+	if (rank == 2) return tex2D<T>(tex, x + 0.5f, y + 0.5f);
+	return tex3D<T>(tex, x + 0.5f, y + 0.5f, z + 0.5f);
+}
+
+__device__ __forceinline__ double texel_as_double(cudaTextureObject_t tex, int dtype, int rank, int x, int y, int z)
+{
+	switch (dtype) {
+	case IANE_GB_U8: return static_cast<double>(texel<unsigned char>(tex, rank, x, y, z));
+	case IANE_GB_I8: return static_cast<double>(texel<signed char>(tex, rank, x, y, z));
+	case IANE_GB_U16: return static_cast<double>(texel<unsigned short>(tex, rank, x, y, z));
+	case IANE_GB_I16: return static_cast<double>(texel<short>(tex, rank, x, y, z));
+	case IANE_GB_I32: return static_cast<double>(texel<int>(tex, rank, x, y, z));
+	case IANE_GB_U32: return static_cast<double>(texel<unsigned int>(tex, rank, x, y, z));
+	case IANE_GB_F32: return static_cast<double>(texel<float>(tex, rank, x, y, z));
+	default: return 0.0;
+	}
+}
+
+// Texture source of a convolution (a normalised iane_gb_texture_view).
+struct TexSource {
+	cudaTextureObject_t tex;
+	int dtype;
+	int rank;
+	int origin[3];
+};
 
 // Border rule for one coordinate: returns false if the sample is the zero value.
 // clamp/zero follow include/iane/locator/image_locator.hpp:44-52; mirror is half-sample

@@ -1,6 +1,7 @@
 // iane_gb_convolve's FP32 fast path: the register-tiled kernel of conv_tile.cuh, with the halo
-// tiles staged by TMA when the source is TMA-addressable (clamp and mirror edges fixed up in
-// shared memory) and by 4-byte cp.async with the border rule applied per element otherwise.
+// tiles staged by TMA when the source is a TMA-addressable f32 view (clamp and mirror edges
+// fixed up in shared memory), by 4-byte cp.async with the border rule applied per element for
+// other f32 views, and by converting loads for other element types and texture sources.
 #pragma once
 
 #include "conv_tile.cuh"
@@ -8,7 +9,7 @@
 namespace iane_gb {
 
 template<int KX>
-int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma,
+int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
 	cudaStream_t stream)
 {
 	TileArgs a{};
@@ -24,6 +25,13 @@ int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst,
 	a.kz = kernel.ext[2];
 	a.kernel = kernel.ptr;
 	a.border = border;
+	if (tex) {
+		a.stage = kStageTexture;
+		a.tex = *tex;
+	} else {
+		a.stage = src.dtype == IANE_GB_F32 ? kStageF32 : kStageConvert;
+		a.src_dtype = src.dtype;
+	}
 	a.status = device_status_ptr();
 	if (!a.status) {
 		return IANE_GB_CUDA_ERROR;
@@ -34,6 +42,7 @@ int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst,
 	epi.nx = dst.ext[0];
 	epi.ny = dst.ext[1];
 	epi.vec4 = rows_aligned16(dst) ? 1 : 0;
+	epi.dtype = dst.dtype;
 	// Large images use 64x64 tiles; small ones 32x32 so that the grid still fills the GPU.
 	const long long big_tiles = static_cast<long long>((a.nx + 63) / 64) * ((a.ny + 63) / 64) * a.nz;
 	const bool big = big_tiles >= 2LL * device_sm_count();
@@ -52,9 +61,9 @@ int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst,
 }
 
 // Kernel widths 1..15 (conv_f32.cu) and 17..31 (conv_f32_wide.cu).
-int launch_f32_narrow(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma,
+int launch_f32_narrow(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
 	cudaStream_t stream);
-int launch_f32_wide(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma,
+int launch_f32_wide(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
 	cudaStream_t stream);
 
 }  // namespace iane_gb

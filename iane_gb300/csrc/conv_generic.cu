@@ -53,26 +53,31 @@ __device__ __forceinline__ double load_coef(const char* p, int dtype)
 	}
 }
 
-__device__ __forceinline__ void store_sum(char* p, int dtype, double sum)
-{
-	switch (dtype) {
-	case IANE_GB_U8: *reinterpret_cast<uint8_t*>(p) = convert_sum<uint8_t>(sum); break;
-	case IANE_GB_U16: *reinterpret_cast<uint16_t*>(p) = convert_sum<uint16_t>(sum); break;
-	case IANE_GB_I16: *reinterpret_cast<int16_t*>(p) = convert_sum<int16_t>(sum); break;
-	case IANE_GB_I32: *reinterpret_cast<int32_t*>(p) = convert_sum<int32_t>(sum); break;
-	case IANE_GB_F32: *reinterpret_cast<float*>(p) = convert_sum<float>(sum); break;
-	case IANE_GB_F64: *reinterpret_cast<double*>(p) = sum; break;
-	default: break;
-	}
-}
-
 struct GenericArgs {
 	DevView src;
 	DevView kernel;
 	DevView dst;
 	int border;
-	int staged; // 1: halo tile in shared memory; 0: direct loads (tile too large)
+	int staged;    // 1: halo tile in shared memory; 0: direct loads (tile too large)
+	int use_tex;   // samples come from `tex` (src gives extents and the texel type only)
+	TexSource tex;
 };
+
+template<class T> inline constexpr bool texel_type = std::is_same_v<T, uint8_t> || std::is_same_v<T, int8_t> ||
+	std::is_same_v<T, uint16_t> || std::is_same_v<T, int16_t> || std::is_same_v<T, int32_t> ||
+	std::is_same_v<T, uint32_t> || std::is_same_v<T, float>;
+
+// Sample (xi, yi, zi) (in range) of the memory view or the texture.
+template<class TS>
+__device__ __forceinline__ TS load_sample(const GenericArgs& a, int xi, int yi, int zi)
+{
+	if constexpr (texel_type<TS>) {
+		if (a.use_tex) {
+			return texel<TS>(a.tex.tex, a.tex.rank, a.tex.origin[0] + xi, a.tex.origin[1] + yi, a.tex.origin[2] + zi);
+		}
+	}
+	return *element_ptr<TS>(a.src, xi, yi, zi);
+}
 
 template<class TS, class TAcc>
 __global__ void __launch_bounds__(kGX * kGY) conv_generic_kernel(GenericArgs a)
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(kGX * kGY) conv_generic_kernel(GenericArgs a)
 				int xi = 0, yi = 0;
 				TS v = zero_value<TS>();
 				if (map_coord(x0 - cx + col, nx, a.border, xi) && map_coord(y0 - cy + row, ny, a.border, yi)) {
-					v = *element_ptr<TS>(a.src, xi, yi, zi);
+					v = load_sample<TS>(a, xi, yi, zi);
 				}
 				tile[i] = v;
 			}
@@ -135,7 +140,7 @@ __global__ void __launch_bounds__(kGX * kGY) conv_generic_kernel(GenericArgs a)
 					int xi = 0, yi = 0;
 					s = TAcc(0);
 					if (map_coord(x + cx - qx, nx, a.border, xi) && map_coord(y + cy - qy, ny, a.border, yi)) {
-						s = ops::sample(*element_ptr<TS>(a.src, xi, yi, zi));
+						s = ops::sample(load_sample<TS>(a, xi, yi, zi));
 					}
 				}
 				acc = ops::mac(s, kp[qy * kx + qx], acc);
@@ -144,7 +149,7 @@ __global__ void __launch_bounds__(kGX * kGY) conv_generic_kernel(GenericArgs a)
 	}
 	if (active) {
 		char* out = a.dst.ptr + x * a.dst.stride[0] + y * a.dst.stride[1] + z * a.dst.stride[2];
-		store_sum(out, a.dst.dtype, ops::to_sum(acc));
+		store_converted(out, a.dst.dtype, ops::to_sum(acc));
 	}
 }
 
@@ -187,9 +192,18 @@ int launch_for_source(const GenericArgs& args, bool exact, cudaStream_t stream)
 }  // namespace
 
 int launch_conv_generic(const DevView& src, const DevView& kernel, const DevView& dst, int border, bool exact,
-	cudaStream_t stream)
+	cudaStream_t stream, const TexSource* tex)
 {
-	GenericArgs a{src, kernel, dst, border, 1};
+	GenericArgs a{};
+	a.src = src;
+	a.kernel = kernel;
+	a.dst = dst;
+	a.border = border;
+	a.staged = 1;
+	if (tex) {
+		a.use_tex = 1;
+		a.tex = *tex;
+	}
 	if (src.ext[1] > 65535 * kGY || src.ext[2] > 65535) {
 		return fail(IANE_GB_UNSUPPORTED, "convolve: image too large along axis 1 or 2 for the grid");
 	}
@@ -201,6 +215,8 @@ int launch_conv_generic(const DevView& src, const DevView& kernel, const DevView
 	case IANE_GB_F32: return launch_for_source<float>(a, exact, stream);
 	case IANE_GB_F64: return launch_for_source<double>(a, exact, stream);
 	case IANE_GB_BF16: return launch_for_source<__nv_bfloat16>(a, exact, stream);
+	case IANE_GB_I8: return launch_for_source<int8_t>(a, exact, stream);
+	case IANE_GB_U32: return launch_for_source<uint32_t>(a, exact, stream);
 	default: return fail(IANE_GB_UNSUPPORTED, "convolve: unsupported source element type");
 	}
 }

@@ -50,11 +50,21 @@ struct TileWidth {
 	static constexpr int P = (W % 8 == 0) ? W + 4 : W;        // pitch, = 4 mod 8 floats
 };
 
+// How the non-TMA path stages a halo tile.
+enum TileStage : int {
+	kStageF32 = 0,     // f32 source, 4-byte cp.async
+	kStageConvert = 1, // any element type (TileArgs::src_dtype), converted to float while loading
+	kStageTexture = 2, // texels of TileArgs::tex, converted to float
+};
+
 struct TileArgs {
-	// source of the halo tiles (f32), used by the cp.async path
+	// source of the halo tiles, used by the non-TMA path (the TMA path reads the tensor map)
 	const char* src;
 	long long s_stride[3];
 	int nx, ny, nz;
+	int stage;     // TileStage
+	int src_dtype; // kStageConvert: element type of src
+	TexSource tex; // kStageTexture: the texture and the view's origin
 	// kernel: kx is the template KX; f32 device view
 	int ky, kz;
 	const char* kernel;
@@ -152,13 +162,30 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 			int zi = 0;
 			const bool zok = map_coord(z + rz - qz, a.nz, a.border, zi);
 			const char* plane = a.src + zi * a.s_stride[2];
-			for (int i = tid; i < W * H; i += NT) {
-				const int col = i % W, row = i / W;
-				int xi = 0, yi = 0;
-				const bool ok = zok && map_coord(x0 - G::RXA + col, a.nx, a.border, xi) &&
-					map_coord(y0 - ry + row, a.ny, a.border, yi);
-				const char* src = ok ? plane + xi * a.s_stride[0] + yi * a.s_stride[1] : a.src;
-				cp_async4(dst + row * P + col, src, ok ? 4 : 0);
+			if (a.stage == kStageF32) {
+				for (int i = tid; i < W * H; i += NT) {
+					const int col = i % W, row = i / W;
+					int xi = 0, yi = 0;
+					const bool ok = zok && map_coord(x0 - G::RXA + col, a.nx, a.border, xi) &&
+						map_coord(y0 - ry + row, a.ny, a.border, yi);
+					const char* src = ok ? plane + xi * a.s_stride[0] + yi * a.s_stride[1] : a.src;
+					cp_async4(dst + row * P + col, src, ok ? 4 : 0);
+				}
+			} else {
+				// plain loads and stores; the wait and barrier before the tile is read order them
+				for (int i = tid; i < W * H; i += NT) {
+					const int col = i % W, row = i / W;
+					int xi = 0, yi = 0;
+					float v = 0.0f;
+					if (zok && map_coord(x0 - G::RXA + col, a.nx, a.border, xi) &&
+					    map_coord(y0 - ry + row, a.ny, a.border, yi)) {
+						v = a.stage == kStageConvert
+							? load_as_float(plane + xi * a.s_stride[0] + yi * a.s_stride[1], a.src_dtype)
+							: static_cast<float>(texel_as_double(a.tex.tex, a.tex.dtype, a.tex.rank, a.tex.origin[0] + xi,
+								a.tex.origin[1] + yi, a.tex.origin[2] + zi));
+					}
+					dst[row * P + col] = v;
+				}
 			}
 			cp_async_commit();
 		}
@@ -323,12 +350,14 @@ int launch_tile(const CUtensorMap& map, const TileArgs& a, const Epi& epi, cudaS
 	return IANE_GB_OK;
 }
 
-// Plain f32 store epilogue for iane_gb_convolve.
+// Store epilogue for iane_gb_convolve: f32 destinations directly (16-byte stores where rows
+// allow), other element types through the reference's conversion of the sum.
 struct EpiStoreF32 {
 	char* dst;
 	long long stride[3];
 	int nx, ny;
-	int vec4; // rows start 16-byte aligned and axis 0 is packed
+	int vec4;   // rows start 16-byte aligned and axis 0 is packed
+	int dtype;  // destination element type (0 or IANE_GB_F32: f32)
 
 	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[kRX]) const
 	{
@@ -336,6 +365,15 @@ struct EpiStoreF32 {
 			return;
 		}
 		char* base = dst + y * stride[1] + z * stride[2];
+		if (dtype != 0 && dtype != IANE_GB_F32) {
+#pragma unroll
+			for (int i = 0; i < kRX; ++i) {
+				if (xo + i < nx) {
+					store_converted(base + (xo + i) * stride[0], dtype, static_cast<double>(v[i]));
+				}
+			}
+			return;
+		}
 		if (vec4 && xo + kRX <= nx) {
 			float4* p = reinterpret_cast<float4*>(base + xo * 4LL);
 			p[0] = make_float4(v[0], v[1], v[2], v[3]);

@@ -33,7 +33,7 @@ extern "C" {
 #define IANE_GB_ABI_VERSION 1
 #define IANE_GB_MAX_RANK 3
 
-/* Element types. f64 is accepted for the exact-accumulation path only. */
+/* Element types. */
 typedef enum iane_gb_dtype {
 	IANE_GB_U8 = 1,
 	IANE_GB_U16 = 2,
@@ -41,7 +41,14 @@ typedef enum iane_gb_dtype {
 	IANE_GB_I32 = 4,
 	IANE_GB_F32 = 5,
 	IANE_GB_F64 = 6,
-	IANE_GB_BF16 = 7
+	IANE_GB_BF16 = 7,
+	IANE_GB_I8 = 8,
+	IANE_GB_U32 = 9,
+	/* Packed 3-byte (r, g, b) pixel. Convolution treats each channel as its own u8 image
+	 * with a float kernel and writes packed pixels: the custom element of the reference's
+	 * convolution example (examples/convolution/main.cu:20-56, a per-channel double sum
+	 * converted with the byte rule). */
+	IANE_GB_RGB8 = 10
 } iane_gb_dtype;
 
 /* Boundary rules. clamp and zero are the reference's border_mode
@@ -106,9 +113,46 @@ int iane_gb_device_status(void* stream);
  * the same extents as src and disjoint from both inputs. The kernel is a device view of
  * the same rank. Results follow the reference's casts (convolution.hpp:51-75):
  * u8 rounds half up and saturates; other integers saturate and map NaN to 0.
- * Supported: src u8/u16/i16/i32/f32/bf16/f64, kernel i32/f32/f64, dst u8/u16/i16/i32/f32/f64.
+ * Supported: src u8/i8/u16/i16/i32/u32/f32/bf16/f64, kernel i32/f32/f64,
+ * dst u8/i8/u16/i16/i32/u32/f32/f64; and rgb8 src and dst with an f32 kernel.
  */
 int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel,
+	const iane_gb_view* dst, int border, unsigned flags, void* stream);
+
+/*
+ * A point-sampled CUDA texture as a convolution source: the reference's
+ * texture_image_view<T, N> (include/iane/view/texture_image_view.hpp:26-98), which reads
+ * texel origin + p at the texel centre. `texture` is a cudaTextureObject_t over a CUDA array
+ * of `dtype` elements (u8, i8, u16, i16, i32, u32 or f32) with unnormalised coordinates,
+ * point filtering and element-type reads, as iane_gb_texture_create makes it (and as the
+ * reference's texture_image does, include/iane/resource/cuda/texture_image.hpp:49-80); the
+ * view covers extent[] texels from origin[] (axis 0 fastest; unused axes ignored).
+ */
+typedef struct iane_gb_texture_view {
+	uint64_t texture;
+	int32_t dtype;
+	int32_t rank;
+	int32_t extent[3];
+	int32_t origin[3];
+} iane_gb_texture_view;
+
+/* The reference's texture_image (include/iane/resource/cuda/texture_image.hpp:20-96): a
+ * CUDA array of `extent` elements of `dtype` and its texture object on the current device.
+ * An empty extent allocates nothing and yields texture 0. */
+int iane_gb_texture_create(int dtype, int rank, const int32_t* extent, uint64_t* texture);
+
+/* Upload a host or device view of the texture's dtype and extents into its array (the
+ * reference's copy(view, texture_image), texture_image.hpp:98-140): rows must be contiguous
+ * (stride[0] = element size), rows and planes may be padded. Asynchronous on `stream`. */
+int iane_gb_texture_upload(uint64_t texture, const iane_gb_view* src, void* stream);
+
+/* Destroy a texture made by iane_gb_texture_create and free its array. Waits for nothing:
+ * the caller keeps it alive until work that reads it has finished. */
+int iane_gb_texture_destroy(uint64_t texture);
+
+/* iane_gb_convolve with a texture source: same formula, borders, flags (exact mode gives the
+ * reference's bits; spectral flags are refused) and destination rules. */
+int iane_gb_convolve_texture(const iane_gb_texture_view* src, const iane_gb_view* kernel,
 	const iane_gb_view* dst, int border, unsigned flags, void* stream);
 
 /*

@@ -103,6 +103,23 @@ def convolve(src: np.ndarray, kernel: np.ndarray, out: np.ndarray, border: str =
     return out
 
 
+def convolve_rgb8(src: np.ndarray, kernel: np.ndarray, out: np.ndarray, border: str = "clamp",
+                  threads: int | None = None, use_reference: bool = False) -> np.ndarray:
+    """convolve() for packed (r, g, b) pixels: uint8 arrays of shape (..., 3), f32 kernel of
+    the image rank (the custom element of examples/convolution/main.cu:20-56)."""
+    threads = default_threads() if threads is None else threads
+    s = abi.rgb8_view(src.ctypes.data, src.shape, src.strides)
+    d = abi.rgb8_view(out.ctypes.data, out.shape, out.strides)
+    k = abi.numpy_view(kernel)
+    if use_reference:
+        status = ref_lib().ref_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), abi.BORDERS[border], threads)
+    else:
+        status = oracle_lib().oracle_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), abi.BORDERS[border],
+                                              threads)
+    _check(status, "convolve rgb8")
+    return out
+
+
 def convolve_separable(src: np.ndarray, taps, out: np.ndarray, border: str = "clamp",
                        threads: int | None = None) -> np.ndarray:
     """Successive 1-D convolutions along axis 0 (fastest), 1, 2 with f32 intermediates.

@@ -72,6 +72,9 @@ static int dtype_size(int dtype)
 	case IANE_GB_F32: return 4;
 	case IANE_GB_F64: return 8;
 	case IANE_GB_BF16: return 2;
+	case IANE_GB_I8: return 1;
+	case IANE_GB_U32: return 4;
+	case IANE_GB_RGB8: return 3;
 	default: return 0;
 	}
 }
@@ -86,6 +89,8 @@ static double load_double(const char* p, int dtype)
 	case IANE_GB_F32: { float v; memcpy(&v, p, 4); return (double)v; }
 	case IANE_GB_F64: { double v; memcpy(&v, p, 8); return v; }
 	case IANE_GB_BF16: { uint16_t v; memcpy(&v, p, 2); return (double)bf16_to_float(v); }
+	case IANE_GB_I8: return (double)*(const int8_t*)p;
+	case IANE_GB_U32: { uint32_t v; memcpy(&v, p, 4); return (double)v; }
 	default: return 0.0;
 	}
 }
@@ -131,6 +136,24 @@ static void store_double(char* p, int dtype, double sum)
 		else if (sum <= -2147483648.0) r = INT32_MIN;
 		else if (sum >= 2147483647.0) r = INT32_MAX;
 		else r = (int32_t)sum;
+		memcpy(p, &r, 4);
+		return;
+	}
+	case IANE_GB_I8: {
+		int8_t r;
+		if (sum != sum) r = 0;
+		else if (sum <= -128.0) r = -128;
+		else if (sum >= 127.0) r = 127;
+		else r = (int8_t)sum;
+		*(int8_t*)p = r;
+		return;
+	}
+	case IANE_GB_U32: {
+		uint32_t r;
+		if (sum != sum) r = 0;
+		else if (sum <= 0.0) r = 0;
+		else if (sum >= 4294967295.0) r = UINT32_MAX;
+		else r = (uint32_t)sum;
 		memcpy(p, &r, 4);
 		return;
 	}
@@ -350,6 +373,25 @@ int oracle_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const i
 		if (src->extent[i] != dst->extent[i]) {
 			return ORACLE_EINVAL;
 		}
+	}
+	if (src->dtype == IANE_GB_RGB8 || dst->dtype == IANE_GB_RGB8) {
+		/* Packed (r, g, b) pixels (examples/convolution/main.cu:20-56): the sum of pixel * tap
+		 * is per channel, each channel's byte-times-f32 product is exact in double, so each
+		 * channel is the u8 convolution of that channel. */
+		if (src->dtype != dst->dtype || kernel->dtype != IANE_GB_F32) {
+			return ORACLE_EINVAL;
+		}
+		for (int c = 0; c < 3; ++c) {
+			iane_gb_view sc = *src, dc = *dst;
+			sc.dtype = dc.dtype = IANE_GB_U8;
+			sc.ptr = (char*)src->ptr + c;
+			dc.ptr = (char*)dst->ptr + c;
+			const int status = oracle_convolve(&sc, kernel, &dc, border, threads);
+			if (status) {
+				return status;
+			}
+		}
+		return ORACLE_OK;
 	}
 	conv_job job;
 	memset(&job, 0, sizeof job);

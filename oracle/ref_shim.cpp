@@ -49,6 +49,47 @@ extents_t<tDim> to_strides(const int64_t* values)
 	return out;
 }
 
+// A packed byte (r, g, b) pixel and its per-channel double sum, with the element semantics of
+// the custom pixel in the reference's convolution example (examples/convolution/main.cu:20-56):
+// the product with a float tap is taken in double per channel, sums add channel by channel,
+// and the conversion back rounds each channel half up and saturates to a byte.
+struct pixel3 {
+	std::uint8_t c[3];
+};
+static_assert(sizeof(pixel3) == 3);
+
+struct pixel3_sum {
+	double c[3];
+
+	pixel3_sum operator+(const pixel3_sum& aOther) const
+	{
+		return {{c[0] + aOther.c[0], c[1] + aOther.c[1], c[2] + aOther.c[2]}};
+	}
+
+	explicit operator pixel3() const
+	{
+		pixel3 out{};
+		for (int i = 0; i < 3; ++i) {
+			const double v = c[i];
+			if (!(v > 0.0)) {
+				out.c[i] = 0;
+			} else if (v >= 255.0) {
+				out.c[i] = 255;
+			} else {
+				const auto whole = static_cast<unsigned int>(v);
+				out.c[i] = static_cast<std::uint8_t>(whole + (v - whole >= 0.5 ? 1u : 0u));
+			}
+		}
+		return out;
+	}
+};
+
+pixel3_sum operator*(pixel3 aPixel, float aTap)
+{
+	const double tap = aTap;
+	return {{aPixel.c[0] * tap, aPixel.c[1] * tap, aPixel.c[2] * tap}};
+}
+
 template<class TSrc, class TKernel, class TDst, int tDim>
 int convolve_typed(const iane_gb_view& aSrc, const iane_gb_view& aKernel, const iane_gb_view& aDst,
 	int aBorder, int aThreads)
@@ -97,6 +138,13 @@ int dispatch(const iane_gb_view& aSrc, const iane_gb_view& aKernel, const iane_g
 	IANE_REF_COMBO(IANE_GB_F32, IANE_GB_F32, IANE_GB_U8, float, float, std::uint8_t)
 	IANE_REF_COMBO(IANE_GB_F32, IANE_GB_F32, IANE_GB_I32, float, float, std::int32_t)
 	IANE_REF_COMBO(IANE_GB_U16, IANE_GB_F32, IANE_GB_F32, std::uint16_t, float, float)
+	IANE_REF_COMBO(IANE_GB_I8, IANE_GB_F32, IANE_GB_I8, std::int8_t, float, std::int8_t)
+	IANE_REF_COMBO(IANE_GB_I8, IANE_GB_I32, IANE_GB_I8, std::int8_t, std::int32_t, std::int8_t)
+	IANE_REF_COMBO(IANE_GB_U32, IANE_GB_F32, IANE_GB_U32, std::uint32_t, float, std::uint32_t)
+	IANE_REF_COMBO(IANE_GB_U32, IANE_GB_I32, IANE_GB_U32, std::uint32_t, std::int32_t, std::uint32_t)
+	IANE_REF_COMBO(IANE_GB_F32, IANE_GB_F32, IANE_GB_I8, float, float, std::int8_t)
+	IANE_REF_COMBO(IANE_GB_F32, IANE_GB_F32, IANE_GB_U32, float, float, std::uint32_t)
+	IANE_REF_COMBO(IANE_GB_RGB8, IANE_GB_F32, IANE_GB_RGB8, pixel3, float, pixel3)
 	return IANE_GB_UNSUPPORTED;
 }
 

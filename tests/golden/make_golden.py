@@ -114,6 +114,31 @@ def main() -> int:
     bench_out = ref_conv(image, kernel, np.uint8, "clamp")
     g["bench_u8_2560x1920__sha256"] = np.array(hashlib.sha256(bench_out.tobytes()).hexdigest())
 
+    # Element types added later, from their own seed so that the arrays above stay as they
+    # were: i8 and u32 scalars, and packed rgb8 pixels (the custom element of
+    # examples/convolution/main.cu:20-56) through the reference's convolve with a pixel type
+    # of those semantics (oracle/ref_shim.cpp).
+    rng2 = np.random.default_rng(20261204)
+    case("i8_2d_f32k_clamp", rng2.integers(-128, 128, (13, 17), dtype=np.int8),
+         rng2.standard_normal((5, 3)).astype(np.float32), np.int8, "clamp")
+    case("i8_3d_i32k_zero", rng2.integers(-128, 128, (4, 7, 9), dtype=np.int8),
+         rng2.integers(-3, 4, (3, 3, 3), dtype=np.int32), np.int8, "zero")
+    case("u32_2d_f32k_zero", rng2.integers(0, 2 ** 32, (9, 11), dtype=np.uint32),
+         rng2.random((3, 5), dtype=np.float32), np.uint32, "zero")
+    case("u32_1d_i32k_clamp", rng2.integers(0, 2 ** 31, 29, dtype=np.uint32),
+         rng2.integers(-2, 5, 7, dtype=np.int32), np.uint32, "clamp")
+    for border in ("clamp", "zero"):
+        rgb = rng2.integers(0, 256, (19, 23, 3), dtype=np.uint8)
+        k = (rng2.standard_normal((5, 7)) / 4.0).astype(np.float32)
+        out = np.zeros_like(rgb)
+        oracle.convolve_rgb8(rgb, k, out, border, use_reference=True)
+        g[f"rgb8_2d_{border}__src"], g[f"rgb8_2d_{border}__kernel"], g[f"rgb8_2d_{border}__out"] = rgb, k, out
+    rgb, k = bench_pattern(64, 48)
+    rgb = np.stack([rgb, rgb[::-1], 255 - rgb], axis=-1).copy()
+    out = np.zeros_like(rgb)
+    oracle.convolve_rgb8(rgb, k, out, "clamp", use_reference=True)
+    g["rgb8_bench_clamp__src"], g["rgb8_bench_clamp__kernel"], g["rgb8_bench_clamp__out"] = rgb, k, out
+
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
     return 0

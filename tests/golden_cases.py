@@ -22,6 +22,14 @@ def conv_cases():
     return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"], str(d[f"{n}__border"])) for n in names]
 
 
+def rgb8_cases():
+    """Packed rgb8 images (h, w, 3) convolved by the reference with a per-channel pixel type;
+    the border is the name's suffix."""
+    d = data()
+    names = sorted({k.split("__")[0] for k in d if k.startswith("rgb8_") and k.endswith("__src")})
+    return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"], n.rsplit("_", 1)[1]) for n in names]
+
+
 def mirror_cases():
     d = data()
     return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"]) for n in ("mirror_2d", "mirror_3d")]

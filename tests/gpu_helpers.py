@@ -22,6 +22,8 @@ def to_gpu(arr: np.ndarray):
     a = np.ascontiguousarray(arr)
     if a.dtype == np.uint16:
         return t.from_numpy(a.view(np.int16)).cuda().view(t.uint16)
+    if a.dtype == np.uint32:
+        return t.from_numpy(a.view(np.int32)).cuda().view(t.uint32)
     return t.from_numpy(a).cuda()
 
 
@@ -30,13 +32,15 @@ def to_host(tensor) -> np.ndarray:
     torch().cuda.synchronize()
     if tensor.dtype == t.uint16:
         return tensor.contiguous().view(t.int16).cpu().numpy().view(np.uint16)
+    if tensor.dtype == t.uint32:
+        return tensor.contiguous().view(t.int32).cpu().numpy().view(np.uint32)
     return tensor.contiguous().cpu().numpy()
 
 
 def empty_like_np(shape, dtype):
     t = torch()
     table = {np.float32: t.float32, np.float64: t.float64, np.uint8: t.uint8, np.int32: t.int32,
-             np.int16: t.int16, np.uint16: t.uint16}
+             np.int16: t.int16, np.uint16: t.uint16, np.int8: t.int8, np.uint32: t.uint32}
     return t.zeros(shape, dtype=table[np.dtype(dtype).type], device="cuda")
 
 

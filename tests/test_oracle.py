@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
-from golden_cases import bench_pattern, conv_cases, mirror_cases, rl_cases
+from golden_cases import bench_pattern, conv_cases, mirror_cases, rgb8_cases, rl_cases
 
 
 def test_known_answer_1d_flip_zero_border():
@@ -50,6 +50,26 @@ def test_oracle_matches_golden_convolution(case):
     out = np.zeros(expected.shape, expected.dtype)
     oracle.convolve(src, kernel, out, border)
     assert np.array_equal(out, expected), name
+
+
+@pytest.mark.parametrize("case", rgb8_cases(), ids=lambda c: c[0])
+def test_oracle_rgb8_matches_golden(case):
+    name, src, kernel, expected, border = case
+    out = np.zeros_like(src)
+    oracle.convolve_rgb8(src, kernel, out, border)
+    assert np.array_equal(out, expected), name
+
+
+def test_oracle_rgb8_is_three_u8_channels():
+    rng = np.random.default_rng(5)
+    rgb = rng.integers(0, 256, (9, 14, 3), dtype=np.uint8)
+    k = rng.standard_normal((3, 5)).astype(np.float32)
+    out = np.zeros_like(rgb)
+    oracle.convolve_rgb8(rgb, k, out, "mirror")
+    for c in range(3):
+        ch = np.zeros((9, 14), np.uint8)
+        oracle.convolve(np.ascontiguousarray(rgb[..., c]), k, ch, "mirror")
+        assert np.array_equal(out[..., c], ch)
 
 
 @pytest.mark.parametrize("case", mirror_cases(), ids=lambda c: c[0])
@@ -125,6 +145,36 @@ def test_oracle_matches_live_reference_strided_views():
     b = np.zeros((7, 8, 40), np.float32)[:, :, ::2][:, :, :18]
     oracle.convolve(src, kernel, a, "clamp")
     oracle.convolve(src, kernel, b, "clamp", use_reference=True)
+    assert np.array_equal(a, b)
+
+
+@reference
+@pytest.mark.parametrize("border", ["clamp", "zero"])
+def test_oracle_rgb8_matches_live_reference(border):
+    rng = np.random.default_rng(17 + len(border))
+    rgb = rng.integers(0, 256, (3, 11, 8, 3), dtype=np.uint8)
+    k = rng.standard_normal((3, 3, 5)).astype(np.float32)
+    a, b = np.zeros_like(rgb), np.zeros_like(rgb)
+    oracle.convolve_rgb8(rgb, k, a, border)
+    oracle.convolve_rgb8(rgb, k, b, border, use_reference=True)
+    assert np.array_equal(a, b)
+
+
+@reference
+@pytest.mark.parametrize("dtypes", [(np.int8, np.float32, np.int8), (np.uint32, np.int32, np.uint32),
+                                    (np.float32, np.float32, np.int8), (np.float32, np.float32, np.uint32)])
+def test_oracle_new_scalar_types_match_live_reference(dtypes):
+    sd, kd, dd = dtypes
+    rng = np.random.default_rng(23)
+    if sd == np.float32:
+        src = (rng.standard_normal((6, 10, 7)) * 3e9).astype(np.float32)
+    else:
+        info = np.iinfo(sd)
+        src = rng.integers(info.min, info.max, (6, 10, 7), dtype=sd, endpoint=True)
+    k = rng.integers(-3, 4, (3, 5, 3)).astype(kd) if kd == np.int32 else rng.standard_normal((3, 5, 3)).astype(kd)
+    a, b = np.zeros(src.shape, dd), np.zeros(src.shape, dd)
+    oracle.convolve(src, k, a, "zero")
+    oracle.convolve(src, k, b, "zero", use_reference=True)
     assert np.array_equal(a, b)
 
 
