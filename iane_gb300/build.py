@@ -59,7 +59,9 @@ def _compile(src: Path, force: bool, verbose: bool) -> Path:
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> Path:
     BUILD.mkdir(exist_ok=True)
-    sources = sorted(CSRC.glob("*.cu"))
+    # the translation units with many kernel instantiations first, so the pool ends together
+    heavy = ("conv_f32_k", "rl_pass", "rl_batch_k")
+    sources = sorted(CSRC.glob("*.cu"), key=lambda p: (not p.stem.startswith(heavy), p.name))
     jobs = jobs or max(1, min(len(sources), os.cpu_count() or 4))
     with ThreadPoolExecutor(max_workers=jobs) as pool:
         objects = list(pool.map(lambda s: _compile(s, force, verbose), sources))

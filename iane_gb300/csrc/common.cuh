@@ -155,6 +155,46 @@ __device__ __forceinline__ void store_converted(char* p, int dtype, double sum)
 	}
 }
 
+// The same conversions for an FP32 sum, in FP32 arithmetic. They equal convert_sum of the
+// sum widened to double: v - (unsigned)v is exact for a float below 2^24, and a float
+// compares with the saturation bounds as its double does once an upper bound that is not a
+// float (2^31 - 1, 2^32 - 1) is replaced by the next float up (no float lies in between).
+__device__ __forceinline__ uint8_t convert_f32_u8(float v)
+{
+	if (!(v > 0.0f)) return 0;
+	if (v >= 255.0f) return 255;
+	const unsigned int integer = static_cast<unsigned int>(v);
+	return static_cast<uint8_t>(integer + (v - static_cast<float>(integer) >= 0.5f));
+}
+template<class TI>
+__device__ __forceinline__ TI saturate_f32(float v, float lo, float hi, TI lov, TI hiv)
+{
+	if (v != v) return TI(0);
+	if (v <= lo) return lov;
+	if (v >= hi) return hiv;
+	return static_cast<TI>(v);
+}
+__device__ __forceinline__ void store_converted_f32(char* p, int dtype, float v)
+{
+	switch (dtype) {
+	case IANE_GB_U8: *reinterpret_cast<uint8_t*>(p) = convert_f32_u8(v); break;
+	case IANE_GB_I8: *reinterpret_cast<int8_t*>(p) = saturate_f32<int8_t>(v, -128.0f, 127.0f, -128, 127); break;
+	case IANE_GB_U16: *reinterpret_cast<uint16_t*>(p) = saturate_f32<uint16_t>(v, 0.0f, 65535.0f, 0, 65535); break;
+	case IANE_GB_I16:
+		*reinterpret_cast<int16_t*>(p) = saturate_f32<int16_t>(v, -32768.0f, 32767.0f, -32768, 32767);
+		break;
+	case IANE_GB_I32:
+		*reinterpret_cast<int32_t*>(p) = saturate_f32<int32_t>(v, -2147483648.0f, 2147483648.0f, INT32_MIN, INT32_MAX);
+		break;
+	case IANE_GB_U32:
+		*reinterpret_cast<uint32_t*>(p) = saturate_f32<uint32_t>(v, 0.0f, 4294967296.0f, 0u, 4294967295u);
+		break;
+	case IANE_GB_F32: *reinterpret_cast<float*>(p) = v; break;
+	case IANE_GB_F64: *reinterpret_cast<double*>(p) = static_cast<double>(v); break;
+	default: break;
+	}
+}
+
 // A texel of a point-sampled texture with unnormalised coordinates, read at its centre as
 // the reference's texture_image_view::operator[] does (texture_image_view.hpp:45-53).
 template<class T>

@@ -1,24 +1,8 @@
-// iane_gb_convolve's FP32 fast path: dispatch, and the instantiations for kernel widths 1..15.
+// iane_gb_convolve's FP32 fast path: eligibility, staging choice and dispatch by kernel width.
 #include "conv_f32.cuh"
 #include "kernels.h"
 
 namespace iane_gb {
-
-int launch_f32_narrow(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
-	cudaStream_t stream)
-{
-	switch (kx) {
-	case 1: return launch_f32_kx<1>(src, kernel, dst, border, tma, tex, stream);
-	case 3: return launch_f32_kx<3>(src, kernel, dst, border, tma, tex, stream);
-	case 5: return launch_f32_kx<5>(src, kernel, dst, border, tma, tex, stream);
-	case 7: return launch_f32_kx<7>(src, kernel, dst, border, tma, tex, stream);
-	case 9: return launch_f32_kx<9>(src, kernel, dst, border, tma, tex, stream);
-	case 11: return launch_f32_kx<11>(src, kernel, dst, border, tma, tex, stream);
-	case 13: return launch_f32_kx<13>(src, kernel, dst, border, tma, tex, stream);
-	case 15: return launch_f32_kx<15>(src, kernel, dst, border, tma, tex, stream);
-	default: return IANE_GB_UNSUPPORTED;
-	}
-}
 
 int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevView& dst, int border,
 	cudaStream_t stream, const TexSource* tex)
@@ -36,16 +20,25 @@ int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevVi
 	// Shared memory holds one or two kernel planes' taps (ky x 32 floats at most) next to the
 	// halo tiles; the planes stream through it, so kz has no limit here.
 	(void)kz;
-	// TMA staging when the source is a TMA-addressable f32 view (16-byte aligned rows and
-	// planes that do not overlap) and, for clamp and mirror, wider than the kernel radius on x
-	// and y (the edge fix-up takes its sources from inside the tile); else per-element staging.
-	const bool tma = !tex && src.dtype == IANE_GB_F32 && rows_aligned16(src) &&
-		(src.ext[1] <= 1 || src.stride[1] >= 4LL * src.ext[0]) &&
-		(src.ext[2] <= 1 || (src.stride[2] > 0 && src.stride[2] >= (src.ext[1] > 1 ? src.stride[1] : 4LL * src.ext[0]) *
+	// TMA staging when the source is a TMA-addressable f32 or 8/16-bit integer view (16-byte
+	// aligned rows and planes that do not overlap) and, for clamp and mirror, wider than the
+	// kernel radius on x and y (the edge fix-up takes its sources from inside the tile); else
+	// element-by-element staging.
+	const bool narrow = src.dtype == IANE_GB_U8 || src.dtype == IANE_GB_I8 || src.dtype == IANE_GB_U16 ||
+		src.dtype == IANE_GB_I16;
+	const long long row_bytes = static_cast<long long>(dtype_size(src.dtype)) * src.ext[0];
+	const bool tma = !tex && (src.dtype == IANE_GB_F32 || narrow) && rows_aligned16(src) &&
+		(src.ext[1] <= 1 || src.stride[1] >= row_bytes) &&
+		(src.ext[2] <= 1 || (src.stride[2] > 0 && src.stride[2] >= (src.ext[1] > 1 ? src.stride[1] : row_bytes) *
 			src.ext[1])) &&
 		(border == IANE_GB_BORDER_ZERO || (src.ext[0] > kx / 2 && src.ext[1] > ky / 2));
-	return kx <= 15 ? launch_f32_narrow(kx, src, kernel, dst, border, tma, tex, stream)
-		: launch_f32_wide(kx, src, kernel, dst, border, tma, tex, stream);
+	const int stage = !tma ? kTileCopy : (narrow ? kTileTmaNarrow : kTileTma);
+	static const LaunchF32Widths by_width[8] = {launch_f32_k1_3, launch_f32_k5_7, launch_f32_k9_11, launch_f32_k13_15,
+		launch_f32_k17_19, launch_f32_k21_23, launch_f32_k25_27, launch_f32_k29_31};
+	if (kx < 1 || kx > 31) {
+		return IANE_GB_UNSUPPORTED;
+	}
+	return by_width[(kx - 1) / 4](kx, src, kernel, dst, border, stage, tex, stream);
 }
 
 }  // namespace iane_gb

@@ -9,8 +9,8 @@
 namespace iane_gb {
 
 template<int KX>
-int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
-	cudaStream_t stream)
+int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst, int border, int stage,
+	const TexSource* tex, cudaStream_t stream)
 {
 	TileArgs a{};
 	a.src = src.ptr;
@@ -25,12 +25,12 @@ int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst,
 	a.kz = kernel.ext[2];
 	a.kernel = kernel.ptr;
 	a.border = border;
+	a.src_dtype = src.dtype;
 	if (tex) {
 		a.stage = kStageTexture;
 		a.tex = *tex;
 	} else {
 		a.stage = src.dtype == IANE_GB_F32 ? kStageF32 : kStageConvert;
-		a.src_dtype = src.dtype;
 	}
 	a.status = device_status_ptr();
 	if (!a.status) {
@@ -47,23 +47,64 @@ int launch_f32_kx(const DevView& src, const DevView& kernel, const DevView& dst,
 	const long long big_tiles = static_cast<long long>((a.nx + 63) / 64) * ((a.ny + 63) / 64) * a.nz;
 	const bool big = big_tiles >= 2LL * device_sm_count();
 	CUtensorMap map{};
-	if (!tma) {
-		return big ? launch_tile<KX, 2, 2, false>(map, a, epi, stream) : launch_tile<KX, 1, 1, false>(map, a, epi, stream);
+	if (stage == kTileTmaNarrow) {
+		// the raw staging buffers come on top of the float tiles: element staging instead where
+		// they would not fit (16-bit images with the widest and tallest kernels)
+		const int es = dtype_size(src.dtype);
+		const size_t need = big ? tile_smem_bytes<KX, 2, 2>(a.ky, a.kz, kTileTmaNarrow, es)
+			: tile_smem_bytes<KX, 1, 1>(a.ky, a.kz, kTileTmaNarrow, es);
+		if (need > 227u * 1024u) stage = kTileCopy;
 	}
-	// box = one halo tile at the shared-memory pitch, as the RL passes load theirs
-	const long long row = src.ext[1] > 1 ? src.stride[1] : ((static_cast<long long>(src.ext[0]) * 4 + 15) & ~15LL);
+	// single-plane kernels on large images: direct summation (fewer registers, more blocks)
+	const bool single = big && a.kz == 1;
+	if (stage == kTileCopy) {
+		return single ? launch_tile<KX, 2, 2, kTileCopy, true>(map, a, epi, stream)
+			: big ? launch_tile<KX, 2, 2, kTileCopy>(map, a, epi, stream)
+			: launch_tile<KX, 1, 1, kTileCopy>(map, a, epi, stream);
+	}
+	// box = one halo tile at the shared-memory pitch (f32) or the raw narrow box
+	const int esize = dtype_size(src.dtype);
+	const long long row = src.ext[1] > 1 ? src.stride[1] : ((static_cast<long long>(src.ext[0]) * esize + 15) & ~15LL);
 	const long long plane = src.ext[2] > 1 ? src.stride[2] : row * src.ext[1];
-	const int box_w = big ? TileWidth<KX, 2>::P : TileWidth<KX, 1>::P;
 	const int box_h = (big ? 64 : 32) + 2 * (a.ky / 2);
-	const int status = encode_tensor_map_f32(&map, src.ptr, src.ext[0], src.ext[1], src.ext[2], row, plane, box_w, box_h);
+	if (stage == kTileTma) {
+		const int box_w = big ? TileWidth<KX, 2>::P : TileWidth<KX, 1>::P;
+		const int status =
+			encode_tensor_map_f32(&map, src.ptr, src.ext[0], src.ext[1], src.ext[2], row, plane, box_w, box_h);
+		if (status) return status;
+		return single ? launch_tile<KX, 2, 2, kTileTma, true>(map, a, epi, stream)
+			: big ? launch_tile<KX, 2, 2, kTileTma>(map, a, epi, stream)
+			: launch_tile<KX, 1, 1, kTileTma>(map, a, epi, stream);
+	}
+	const int box_w = big ? narrow_box_elems<KX, 2>(esize) : narrow_box_elems<KX, 1>(esize);
+	const int status = encode_tensor_map(&map, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16,
+		src.ptr, src.ext[0], src.ext[1], src.ext[2], row, plane, box_w, box_h);
 	if (status) return status;
-	return big ? launch_tile<KX, 2, 2, true>(map, a, epi, stream) : launch_tile<KX, 1, 1, true>(map, a, epi, stream);
+	return single ? launch_tile<KX, 2, 2, kTileTmaNarrow, true>(map, a, epi, stream)
+		: big ? launch_tile<KX, 2, 2, kTileTmaNarrow>(map, a, epi, stream)
+		: launch_tile<KX, 1, 1, kTileTmaNarrow>(map, a, epi, stream);
 }
 
-// Kernel widths 1..15 (conv_f32.cu) and 17..31 (conv_f32_wide.cu).
-int launch_f32_narrow(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
-	cudaStream_t stream);
-int launch_f32_wide(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, bool tma, const TexSource* tex,
-	cudaStream_t stream);
+// The instantiations for kernel widths K1 and K2, one pair per translation unit
+// (conv_f32_k*.cu) so that they compile in parallel.
+#define IANE_GB_F32_WIDTHS(NAME, K1, K2)                                                                      \
+	int NAME(int kx, const DevView& src, const DevView& kernel, const DevView& dst, int border, int stage,    \
+		const TexSource* tex, cudaStream_t stream)                                                           \
+	{                                                                                                         \
+		if (kx == K1) return launch_f32_kx<K1>(src, kernel, dst, border, stage, tex, stream);                 \
+		if (kx == K2) return launch_f32_kx<K2>(src, kernel, dst, border, stage, tex, stream);                 \
+		return IANE_GB_UNSUPPORTED;                                                                           \
+	}
+
+using LaunchF32Widths = int (*)(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*,
+	cudaStream_t);
+int launch_f32_k1_3(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k5_7(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k9_11(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k13_15(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k17_19(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k21_23(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k25_27(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
+int launch_f32_k29_31(int, const DevView&, const DevView&, const DevView&, int, int, const TexSource*, cudaStream_t);
 
 }  // namespace iane_gb

@@ -9,7 +9,10 @@
 //     floats, is staged in shared memory -- by one TMA (cp.async.bulk.tensor, zero fill
 //     outside the image; for clamp and mirror borders, tiles at the image edge then rewrite
 //     their out-of-image cells from the cells the rule maps them to) when the buffer is
-//     TMA-addressable, else by 4-byte cp.async with the border rule applied per element --
+//     TMA-addressable (STAGE kTileTma; for 8- and 16-bit integer images, kTileTmaNarrow, the
+//     TMA lands the tile's raw elements in a byte staging buffer and the block converts them
+//     to floats), else element by element with the border rule applied (kTileCopy: 4-byte
+//     cp.async for f32, batched loads and conversion for other element types and textures) --
 //     double buffered, so the next plane lands while this one is consumed;
 //   * a lane walks the RY + 2 ry input rows it needs; each row segment (8 + 2 rx floats) is
 //     read once with 128-bit shared loads into registers and feeds every (output row j,
@@ -21,7 +24,9 @@
 //     64x64-tile blocks fit per SM.
 // Per kernel plane each output accumulates its ky*kx taps into a plane partial that is
 // added to the total afterwards (two-level FP32 summation), which keeps the rounding error
-// of a 1575-tap sum near 1e-6 relative.
+// of a 1575-tap sum near 1e-6 relative. Single-plane kernels (SINGLE) sum straight into the
+// total: the same bits (the total would be +0 + the plane partial, and a sum that starts at
+// +0 is never -0) with 32 fewer live registers, so more blocks fit per SM.
 //
 // Coordinates follow the reference's convolution_filter (include/iane/algorithms/
 // convolution.hpp:37-45): out[p] = sum_q K[q] * in[p + size/2 - q].
@@ -50,7 +55,26 @@ struct TileWidth {
 	static constexpr int P = (W % 8 == 0) ? W + 4 : W;        // pitch, = 4 mod 8 floats
 };
 
-// How the non-TMA path stages a halo tile.
+// How halo tiles reach shared memory (the STAGE template argument).
+constexpr int kTileCopy = 0;       // element by element (TileArgs::stage says how)
+constexpr int kTileTma = 1;        // one TMA of f32 elements
+constexpr int kTileTmaNarrow = 2;  // one TMA of 8- or 16-bit integers, converted in shared memory
+
+// Narrow TMA boxes start 16 elements left of the tile (a 16-byte-aligned x for 1- and 2-byte
+// elements) and cover the float tile's W columns from G::RXA left of it.
+template<int KX, int WX>
+__host__ __device__ constexpr int narrow_box_elems(int esize)
+{
+	return (((16 - TileGeom<KX>::RXA + TileWidth<KX, WX>::W) * esize + 15) & ~15) / esize;
+}
+template<int KX, int WX, int WY>
+__host__ __device__ inline size_t narrow_stage_bytes(int ky, int esize)
+{
+	const int H = 32 * WY + 2 * (ky / 2);
+	return (static_cast<size_t>(narrow_box_elems<KX, WX>(esize)) * esize * H + 127) & ~size_t(127);
+}
+
+// How the element-by-element path stages a halo tile.
 enum TileStage : int {
 	kStageF32 = 0,     // f32 source, 4-byte cp.async
 	kStageConvert = 1, // any element type (TileArgs::src_dtype), converted to float while loading
@@ -77,22 +101,164 @@ struct TileArgs {
 // one for single-plane kernels, which have nothing to double-buffer.
 __host__ __device__ inline int tile_buffers(int kz) { return kz > 1 ? 2 : 1; }
 
-// Shared memory bytes of one launch.
+// Shared memory bytes of one launch: float tiles and taps, the two tile mbarriers and, for
+// kTileTmaNarrow (esize = element bytes), the staging buffers 128 bytes after the barriers.
 template<int KX, int WX, int WY>
-inline size_t tile_smem_bytes(int ky, int kz)
+inline size_t tile_smem_bytes(int ky, int kz, int stage = kTileCopy, int esize = 0)
 {
 	const int H = 32 * WY + 2 * (ky / 2);
 	const size_t plane = (static_cast<size_t>(TileWidth<KX, WX>::P) * H * 4 + 127) & ~size_t(127);
 	const size_t psf = (static_cast<size_t>(ky) * TileGeom<KX>::KXP * 4 + 127) & ~size_t(127);
-	return tile_buffers(kz) * (plane + psf) + 16;
+	const size_t base = tile_buffers(kz) * (plane + psf);
+	if (stage == kTileTmaNarrow) {
+		return base + 128 + tile_buffers(kz) * narrow_stage_bytes<KX, WX, WY>(ky, esize);
+	}
+	return base + 16;
+}
+
+// Element-by-element staging for element types other than f32 and for textures: batches of
+// loads are issued before any is stored so that their latencies overlap; integer and bf16
+// elements are loaded raw by size and converted afterwards.
+template<int W, int P, int NT>
+__device__ __forceinline__ void stage_elements(const TileArgs& a, float* dst, int gx0, int gy0, int H, int zi, bool zok)
+{
+	constexpr int kBatch = 8;
+	const int tid = threadIdx.x;
+	const int n = W * H;
+	const char* plane = a.src + zi * a.s_stride[2];
+	const bool texture = a.stage == kStageTexture;
+	const int esize = a.src_dtype == IANE_GB_U8 || a.src_dtype == IANE_GB_I8 ? 1 :
+		(a.src_dtype == IANE_GB_U16 || a.src_dtype == IANE_GB_I16 || a.src_dtype == IANE_GB_BF16 ? 2 : 4);
+	for (int base = tid; base < n; base += NT * kBatch) {
+		uint32_t raw[kBatch]; // element bits, or a texel's float bits
+		uint32_t in = 0;      // bit u: sample u lies in the image (else it is the zero value)
+#pragma unroll
+		for (int u = 0; u < kBatch; ++u) {
+			const int i = base + u * NT;
+			raw[u] = 0;
+			if (i < n) {
+				const int r = i / W, c = i - (i / W) * W;
+				int xi = 0, yi = 0;
+				if (zok && map_coord(gx0 + c, a.nx, a.border, xi) && map_coord(gy0 + r, a.ny, a.border, yi)) {
+					in |= 1u << u;
+					if (texture) {
+						raw[u] = __float_as_uint(static_cast<float>(texel_as_double(a.tex.tex, a.tex.dtype, a.tex.rank,
+							a.tex.origin[0] + xi, a.tex.origin[1] + yi, a.tex.origin[2] + zi)));
+					} else {
+						const char* q = plane + xi * a.s_stride[0] + yi * a.s_stride[1];
+						raw[u] = esize == 1 ? static_cast<uint32_t>(*reinterpret_cast<const uint8_t*>(q))
+							: esize == 2 ? static_cast<uint32_t>(*reinterpret_cast<const uint16_t*>(q))
+							: *reinterpret_cast<const uint32_t*>(q);
+					}
+				}
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kBatch; ++u) {
+			const int i = base + u * NT;
+			if (i >= n) break;
+			float v = 0.0f;
+			if (in & (1u << u)) {
+				const int dt = texture ? IANE_GB_F32 : a.src_dtype;
+				switch (dt) {
+				case IANE_GB_U8: case IANE_GB_U16: case IANE_GB_U32: v = static_cast<float>(raw[u]); break;
+				case IANE_GB_I8: v = static_cast<float>(static_cast<int8_t>(raw[u])); break;
+				case IANE_GB_I16: v = static_cast<float>(static_cast<int16_t>(raw[u])); break;
+				case IANE_GB_I32: v = static_cast<float>(static_cast<int32_t>(raw[u])); break;
+				case IANE_GB_BF16: v = __uint_as_float(raw[u] << 16); break;
+				default: v = __uint_as_float(raw[u]); break; // f32 bits
+				}
+			}
+			const int r = i / W, c = i - (i / W) * W;
+			dst[r * P + c] = v;
+		}
+	}
+}
+
+// kTileTmaNarrow: convert the raw staged box (row pitch `pitch` bytes) into the float tile.
+template<int W, int P, int NT, int OFF>
+__device__ __forceinline__ void convert_narrow(const unsigned char* sg, float* t, int H, int pitch, int dtype)
+{
+	const int tid = threadIdx.x;
+	switch (dtype) {
+	case IANE_GB_U8:
+		for (int i = tid; i < W * H; i += NT) {
+			const int r = i / W, c = i - r * W;
+			t[r * P + c] = static_cast<float>(sg[r * pitch + OFF + c]);
+		}
+		break;
+	case IANE_GB_I8:
+		for (int i = tid; i < W * H; i += NT) {
+			const int r = i / W, c = i - r * W;
+			t[r * P + c] = static_cast<float>(static_cast<int8_t>(sg[r * pitch + OFF + c]));
+		}
+		break;
+	case IANE_GB_U16:
+		for (int i = tid; i < W * H; i += NT) {
+			const int r = i / W, c = i - r * W;
+			t[r * P + c] = static_cast<float>(reinterpret_cast<const uint16_t*>(sg + r * pitch)[OFF + c]);
+		}
+		break;
+	default: // IANE_GB_I16
+		for (int i = tid; i < W * H; i += NT) {
+			const int r = i / W, c = i - r * W;
+			t[r * P + c] = static_cast<float>(reinterpret_cast<const int16_t*>(sg + r * pitch)[OFF + c]);
+		}
+		break;
+	}
+}
+
+// One kernel plane's taps applied to a lane's kRY x kRX outputs: `tile` is the lane's corner
+// of the halo tile (pitch P floats), `kplane` the plane's taps (rows of KXP floats).
+template<int KX, int P>
+__device__ __forceinline__ void plane_sums(float (&sum)[kRY][kRX], const float* tile, const float* kplane, int ry, int ky)
+{
+	using G = TileGeom<KX>;
+	const int rows = kRY + 2 * ry;
+#pragma unroll 1
+	for (int r = 0; r < rows; ++r) {
+		float seg[G::SEGN];
+		const float4* srow = reinterpret_cast<const float4*>(tile + r * P);
+#pragma unroll
+		for (int m = 0; m < G::SEGN / 4; ++m) {
+			const float4 v = srow[m];
+			seg[4 * m + 0] = v.x;
+			seg[4 * m + 1] = v.y;
+			seg[4 * m + 2] = v.z;
+			seg[4 * m + 3] = v.w;
+		}
+#pragma unroll
+		for (int j = 0; j < kRY; ++j) {
+			const int b = j + 2 * ry - r;
+			if (b >= 0 && b < ky) {
+				const float4* krow = reinterpret_cast<const float4*>(kplane + b * G::KXP);
+				float k[G::KXP];
+#pragma unroll
+				for (int m = 0; m < G::KXP / 4; ++m) {
+					const float4 v = krow[m];
+					k[4 * m + 0] = v.x;
+					k[4 * m + 1] = v.y;
+					k[4 * m + 2] = v.z;
+					k[4 * m + 3] = v.w;
+				}
+#pragma unroll
+				for (int q = 0; q < KX; ++q) {
+#pragma unroll
+					for (int i = 0; i < kRX; ++i) {
+						sum[j][i] = fmaf(k[q], seg[G::D + i + 2 * G::rx - q], sum[j][i]);
+					}
+				}
+			}
+		}
+	}
 }
 
 // One output tile (x0, y0, z) of the tiled convolution. Persistent kernels call it once per
 // work item; `phases` carries the parity of the next wait on each tile buffer's mbarrier
 // (bit b for buffer b) from one call to the next, and `bars` are initialised by the caller.
 // The epilogue's row() runs here; its finish() is the caller's. `bars` are the two tile
-// mbarriers (TMA path), initialised by the caller.
-template<int KX, int WX, int WY, bool TMA, class Epi>
+// mbarriers (TMA stages), initialised by the caller.
+template<int KX, int WX, int WY, int STAGE, class Epi, bool SINGLE = false>
 __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, const TileArgs& a, Epi& epi, int x0,
 	int y0, int z, uint32_t& phases, uint64_t* bars)
 {
@@ -114,6 +280,11 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 
 	const int tid = threadIdx.x;
 	const int lane = tid & 31, warp = tid >> 5;
+	// kTileTmaNarrow: raw boxes of narrow_pitch bytes per row, 128 bytes after the barriers
+	unsigned char* narrow = reinterpret_cast<unsigned char*>(bars) + 128;
+	const int esize = (a.src_dtype == IANE_GB_U8 || a.src_dtype == IANE_GB_I8) ? 1 : 2;
+	const int narrow_pitch = narrow_box_elems<KX, WX>(esize) * esize;
+	const int narrow_buf = static_cast<int>(narrow_stage_bytes<KX, WX, WY>(ky, esize));
 	const int tx_b = (warp % WX) * 4 + (lane & 3);
 	const int ty_b = (warp / WX) * 8 + (lane >> 2);
 
@@ -147,7 +318,7 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 	auto issue = [&](int p) {
 		float* dst = tiles + (p & 1) * plane_floats;
 		const int qz = qz_lo + p;
-		if constexpr (TMA) {
+		if constexpr (STAGE != kTileCopy) {
 			if (tid == 0) {
 				// zero border: an out-of-volume plane is never issued (qz range above); clamp
 				// and mirror: the plane the rule maps to
@@ -155,8 +326,13 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 				if (a.border != IANE_GB_BORDER_ZERO) map_coord(z + rz - qz, a.nz, a.border, zi);
 				// order earlier generic-proxy use of this buffer before the async-proxy write
 				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-				mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(P * H * 4));
-				tma_load_3d(dst, tmap_ptr, x0 - G::RXA, y0 - ry, zi, &bars[p & 1]);
+				if constexpr (STAGE == kTileTma) {
+					mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(P * H * 4));
+					tma_load_3d(dst, tmap_ptr, x0 - G::RXA, y0 - ry, zi, &bars[p & 1]);
+				} else {
+					mbar_arrive_expect_tx(&bars[p & 1], static_cast<uint32_t>(narrow_pitch * H));
+					tma_load_3d(narrow + (p & 1) * narrow_buf, tmap_ptr, x0 - 16, y0 - ry, zi, &bars[p & 1]);
+				}
 			}
 		} else {
 			int zi = 0;
@@ -173,19 +349,7 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 				}
 			} else {
 				// plain loads and stores; the wait and barrier before the tile is read order them
-				for (int i = tid; i < W * H; i += NT) {
-					const int col = i % W, row = i / W;
-					int xi = 0, yi = 0;
-					float v = 0.0f;
-					if (zok && map_coord(x0 - G::RXA + col, a.nx, a.border, xi) &&
-					    map_coord(y0 - ry + row, a.ny, a.border, yi)) {
-						v = a.stage == kStageConvert
-							? load_as_float(plane + xi * a.s_stride[0] + yi * a.s_stride[1], a.src_dtype)
-							: static_cast<float>(texel_as_double(a.tex.tex, a.tex.dtype, a.tex.rank, a.tex.origin[0] + xi,
-								a.tex.origin[1] + yi, a.tex.origin[2] + zi));
-					}
-					dst[row * P + col] = v;
-				}
+				stage_elements<W, P, NT>(a, dst, x0 - G::RXA, y0 - ry, H, zi, zok);
 			}
 			cp_async_commit();
 		}
@@ -202,18 +366,23 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 	// out-of-image cells within (rx, ry) of the image -- the only ones stored outputs read --
 	// from the in-image cells the rule maps them to. Those lie inside the tile whenever
 	// nx > rx and ny > ry (the launcher's condition); any other cell keeps the TMA's zeros.
-	const bool fix_tile = TMA && a.border != IANE_GB_BORDER_ZERO &&
+	const bool fix_tile = STAGE != kTileCopy && a.border != IANE_GB_BORDER_ZERO &&
 		!(x0 - G::RXA >= 0 && x0 - G::RXA + W <= a.nx && y0 - ry >= 0 && y0 + TY + ry <= a.ny);
 	if (nplanes > 0) issue(0);
 	if (nplanes > 1) issue(1);
 	for (int p = 0; p < nplanes; ++p) {
-		if constexpr (TMA) {
+		if constexpr (STAGE != kTileCopy) {
 			const uint32_t bit = 1u << (p & 1);
 			if (ok && !mbar_wait_bounded(&bars[p & 1], (phases & bit) ? 1u : 0u)) {
 				ok = false;
 				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
 			phases ^= bit;
+			if constexpr (STAGE == kTileTmaNarrow) {
+				convert_narrow<W, P, NT, 16 - G::RXA>(narrow + (p & 1) * narrow_buf, tiles + (p & 1) * plane_floats, H,
+					narrow_pitch, a.src_dtype);
+				__syncthreads(); // converted tile visible to all lanes
+			}
 			if (fix_tile) {
 				float* t = tiles + (p & 1) * plane_floats;
 				const int gx0 = x0 - G::RXA, gy0 = y0 - ry;
@@ -242,53 +411,21 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 		}
 		const float* tile = tiles + (p & 1) * plane_floats + (kRY * ty_b) * P + kRX * tx_b;
 		const float* kplane = psf_s + (p & 1) * psf_floats;
-		float part[kRY][kRX];
+		if constexpr (SINGLE) {
+			plane_sums<KX, P>(acc, tile, kplane, ry, ky);
+		} else {
+			float part[kRY][kRX];
 #pragma unroll
-		for (int j = 0; j < kRY; ++j)
+			for (int j = 0; j < kRY; ++j)
 #pragma unroll
-			for (int i = 0; i < kRX; ++i) part[j][i] = 0.0f;
-
-		const int rows = kRY + 2 * ry;
-#pragma unroll 1
-		for (int r = 0; r < rows; ++r) {
-			float seg[G::SEGN];
-			const float4* srow = reinterpret_cast<const float4*>(tile + r * P);
+				for (int i = 0; i < kRX; ++i) part[j][i] = 0.0f;
+			plane_sums<KX, P>(part, tile, kplane, ry, ky);
 #pragma unroll
-			for (int m = 0; m < G::SEGN / 4; ++m) {
-				const float4 v = srow[m];
-				seg[4 * m + 0] = v.x;
-				seg[4 * m + 1] = v.y;
-				seg[4 * m + 2] = v.z;
-				seg[4 * m + 3] = v.w;
-			}
+			for (int j = 0; j < kRY; ++j)
 #pragma unroll
-			for (int j = 0; j < kRY; ++j) {
-				const int b = j + 2 * ry - r;
-				if (b >= 0 && b < ky) {
-					const float4* krow = reinterpret_cast<const float4*>(kplane + b * G::KXP);
-					float k[G::KXP];
-#pragma unroll
-					for (int m = 0; m < G::KXP / 4; ++m) {
-						const float4 v = krow[m];
-						k[4 * m + 0] = v.x;
-						k[4 * m + 1] = v.y;
-						k[4 * m + 2] = v.z;
-						k[4 * m + 3] = v.w;
-					}
-#pragma unroll
-					for (int q = 0; q < KX; ++q) {
-#pragma unroll
-						for (int i = 0; i < kRX; ++i) {
-							part[j][i] = fmaf(k[q], seg[G::D + i + 2 * G::rx - q], part[j][i]);
-						}
-					}
-				}
-			}
+				for (int i = 0; i < kRX; ++i) acc[j][i] += part[j][i];
 		}
-#pragma unroll
-		for (int j = 0; j < kRY; ++j)
-#pragma unroll
-			for (int i = 0; i < kRX; ++i) acc[j][i] += part[j][i];
+
 
 		__syncthreads(); // every lane is done with this plane's tile and taps
 		if (p + 2 < nplanes) {
@@ -317,11 +454,11 @@ __device__ __forceinline__ uint64_t* tile_barriers(int ky, int kz)
 		tile_buffers(kz) * (plane_floats + psf_floats));
 }
 
-template<int KX, int WX, int WY, bool TMA, class Epi>
+template<int KX, int WX, int WY, int STAGE, class Epi, bool SINGLE>
 __global__ void __launch_bounds__(32 * WX * WY)
 	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const Epi epi_in)
 {
-	if constexpr (TMA) {
+	if constexpr (STAGE != kTileCopy) {
 		if (threadIdx.x == 0) {
 			uint64_t* bars = tile_barriers<KX, WX, WY>(a.ky, a.kz);
 			mbar_init(&bars[0], 1);
@@ -331,17 +468,18 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	}
 	Epi epi = epi_in;
 	uint32_t phases = 0;
-	conv_tile_body<KX, WX, WY, TMA, Epi>(&tmap, a, epi, blockIdx.x * 32 * WX, blockIdx.y * 32 * WY, blockIdx.z, phases,
+	conv_tile_body<KX, WX, WY, STAGE, Epi, SINGLE>(&tmap, a, epi, blockIdx.x * 32 * WX, blockIdx.y * 32 * WY, blockIdx.z, phases,
 		tile_barriers<KX, WX, WY>(a.ky, a.kz));
 	epi.finish();
 }
 
 // Launch helper: grid = tiles over (x, y) and one block per output plane.
-template<int KX, int WX, int WY, bool TMA, class Epi>
+template<int KX, int WX, int WY, int STAGE, bool SINGLE = false, class Epi>
 int launch_tile(const CUtensorMap& map, const TileArgs& a, const Epi& epi, cudaStream_t stream)
 {
-	auto kernel = conv_tile_kernel<KX, WX, WY, TMA, Epi>;
-	const size_t smem = tile_smem_bytes<KX, WX, WY>(a.ky, a.kz);
+	auto kernel = conv_tile_kernel<KX, WX, WY, STAGE, Epi, SINGLE>;
+	const int esize = (a.src_dtype == IANE_GB_U8 || a.src_dtype == IANE_GB_I8) ? 1 : 2;
+	const size_t smem = tile_smem_bytes<KX, WX, WY>(a.ky, a.kz, STAGE, esize);
 	IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
 		"tiled convolution: set shared memory size");
 	const dim3 grid((a.nx + 32 * WX - 1) / (32 * WX), (a.ny + 32 * WY - 1) / (32 * WY), a.nz);
@@ -366,10 +504,18 @@ struct EpiStoreF32 {
 		}
 		char* base = dst + y * stride[1] + z * stride[2];
 		if (dtype != 0 && dtype != IANE_GB_F32) {
+			if (dtype == IANE_GB_U8 && vec4 && xo + kRX <= nx) {
+				// packed rows: the lane's 8 bytes in one 8-byte store
+				uint32_t w[2] = {0u, 0u};
+#pragma unroll
+				for (int i = 0; i < kRX; ++i) w[i >> 2] |= static_cast<uint32_t>(convert_f32_u8(v[i])) << (8 * (i & 3));
+				*reinterpret_cast<uint2*>(base + xo) = make_uint2(w[0], w[1]);
+				return;
+			}
 #pragma unroll
 			for (int i = 0; i < kRX; ++i) {
 				if (xo + i < nx) {
-					store_converted(base + (xo + i) * stride[0], dtype, static_cast<double>(v[i]));
+					store_converted_f32(base + (xo + i) * stride[0], dtype, v[i]);
 				}
 			}
 			return;

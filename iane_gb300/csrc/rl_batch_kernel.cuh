@@ -17,7 +17,7 @@ __device__ __forceinline__ void batch_run_item(const BatchImage& im, Epi& epi, i
 	const TileArgs& a = PASS_B ? im.pass_b : im.pass_a;
 	switch (im.kx) {
 #define IANE_GB_BATCH_KX(K) \
-	case K: conv_tile_body<K, WX, WX, true, Epi>(map, a, epi, x0, y0, 0, phases, bars); break;
+	case K: conv_tile_body<K, WX, WX, kTileTma, Epi, true>(map, a, epi, x0, y0, 0, phases, bars); break;
 	IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
 	IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
 	IANE_GB_BATCH_KX(17) IANE_GB_BATCH_KX(19) IANE_GB_BATCH_KX(21) IANE_GB_BATCH_KX(23)
