@@ -5,12 +5,14 @@
 //
 //     iane::convolve(src, kernel, dst, {.border = iane::border_mode::zero}, iane::cuda_policy{stream});
 //
-// on CUDA memory views (const_device_image_view / device_image_view) of u8, u16, i16, i32,
-// f32 or f64 elements, rank 1 to 3, then resolve to the overload below, which carries the
+// on CUDA memory views (const_device_image_view / device_image_view) of u8, i8, u16, i16,
+// i32, u32, f32 or f64 elements (or a packed rgb8 pixel type opted in through
+// iane::gb::packed_rgb8), rank 1 to 3, then resolve to the overload below, which carries the
 // reference template's constraints (include/iane/algorithms/convolution.hpp:91-96) plus
 // native_view on all three views and therefore wins overload resolution as the more
-// constrained candidate. Texture views, procedural views, custom element types and host
-// views keep resolving to the reference's generic template. The call is asynchronous on
+// constrained candidate; texture_image_view sources with memory kernels and destinations
+// resolve to the texture overload at the end. Procedural views, other custom element types
+// and host views keep resolving to the reference's generic template. The call is asynchronous on
 // the policy's stream, returns an execution handle whose wait() synchronises it, and
 // reports errors with the reference's exception types: std::invalid_argument for kernel
 // extents that are not positive and odd or for mismatched image extents, std::runtime_error
@@ -25,8 +27,11 @@
 #pragma once
 
 #include <iane/algorithms/convolution.hpp>
+#include <iane/algorithms/copy.hpp>
 #include <iane/execution/context.hpp>
 #include <iane/execution/prepared.hpp>
+#include <iane/view/make_view.hpp>
+#include <iane/view/texture_image_view.hpp>
 #include <iane_gb/capi.h>
 
 #include <cstddef>
@@ -73,19 +78,43 @@ template<> inline constexpr int dtype_code<std::int16_t> = IANE_GB_I16;
 template<> inline constexpr int dtype_code<std::int32_t> = IANE_GB_I32;
 template<> inline constexpr int dtype_code<float> = IANE_GB_F32;
 template<> inline constexpr int dtype_code<double> = IANE_GB_F64;
+template<> inline constexpr int dtype_code<std::int8_t> = IANE_GB_I8;
+template<> inline constexpr int dtype_code<std::uint32_t> = IANE_GB_U32;
+
+} // namespace detail
+
+/// Opt-in for a user's packed byte (r, g, b) pixel type: specialise to std::true_type for a
+/// 3-byte type whose product with a float tap is a per-channel double sum converted back with
+/// the byte rule, like the pixel of the reference's convolution example
+/// (examples/convolution/main.cu:20-56). Views of it then take the GB300 rgb8 path.
+template<class T>
+struct packed_rgb8 : std::false_type {};
+
+namespace detail {
+
+template<class T>
+constexpr int element_code()
+{
+	if constexpr (packed_rgb8<T>::value) {
+		static_assert(sizeof(T) == 3, "a packed rgb8 pixel is 3 bytes");
+		return IANE_GB_RGB8;
+	} else {
+		return dtype_code<T>;
+	}
+}
 
 /// A CUDA memory view whose element type and rank the GB300 kernels take.
 template<class TView>
 concept native_view = concepts::DeviceView<TView> && concepts::MemoryView<TView> &&
 	(TView::dimension >= 1) && (TView::dimension <= IANE_GB_MAX_RANK) &&
-	(dtype_code<std::remove_cv_t<typename TView::value_type>> != 0);
+	(element_code<std::remove_cv_t<typename TView::value_type>>() != 0);
 
 template<class TView>
 iane_gb_view to_view(const TView& aView)
 {
 	iane_gb_view v{};
 	v.ptr = const_cast<void*>(static_cast<const void*>(aView.pointer()));
-	v.dtype = dtype_code<std::remove_cv_t<typename TView::value_type>>;
+	v.dtype = element_code<std::remove_cv_t<typename TView::value_type>>();
 	v.rank = TView::dimension;
 	const auto size = aView.dimensions();
 	const auto strides = aView.strides();
@@ -240,5 +269,43 @@ gb::execution convolve(TSrc aSource, TKernel aKernel, TDst aDestination,
 		aPolicy.stream));
 	return {{aPolicy.stream}};
 }
+
+#if defined(__CUDACC__)
+/**
+ * @brief GB300 convolution with a texture source (texture_image_view, rank 1-3, of a scalar
+ * texel type), a CUDA memory kernel and destination.
+ *
+ * The view keeps its texture object private, so the texels are first gathered into a
+ * stream-ordered linear buffer by the reference's own copy (texture_image_view::operator[],
+ * include/iane/view/texture_image_view.hpp:45-53) and the buffer is convolved by the GB300
+ * kernels; the buffer is freed in stream order. Callers that hold the texture object use
+ * iane_gb_convolve_texture, which reads the texels directly.
+ */
+template<class TElement, int tDim, class TKernel, class TDst>
+requires (gb::detail::native_view<TKernel> && gb::detail::native_view<TDst> &&
+	TKernel::dimension == tDim && TDst::dimension == tDim &&
+	(gb::detail::dtype_code<TElement> != 0) &&
+	concepts::ConvolutionElements<TElement, typename TKernel::value_type, typename TDst::value_type>)
+gb::execution convolve(texture_image_view<TElement, tDim> aSource, TKernel aKernel, TDst aDestination,
+	convolution_options aOptions = {}, view_policy<TDst> aPolicy = {})
+{
+	const auto size = aSource.dimensions();
+	const auto count = math::detail::element_count<tDim>(size);
+	if (count == 0) {
+		return convolve(device::make_const_view<TElement, tDim>(nullptr, size), aKernel, aDestination, aOptions,
+			aPolicy);
+	}
+	TElement* linear = nullptr;
+	detail::check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&linear), count * sizeof(TElement), aPolicy.stream),
+		"GB300 texture convolution: gather buffer");
+	struct release {
+		TElement* ptr;
+		cudaStream_t stream;
+		~release() { cudaFreeAsync(ptr, stream); }
+	} guard{linear, aPolicy.stream};
+	copy(aSource, device::make_view<TElement, tDim>(linear, size), cuda_policy{.stream = aPolicy.stream});
+	return convolve(device::make_const_view<TElement, tDim>(linear, size), aKernel, aDestination, aOptions, aPolicy);
+}
+#endif
 
 } // namespace iane

@@ -14,6 +14,31 @@
 #include <type_traits>
 #include <utility>
 
+// A packed byte pixel with per-channel double sums (the element of the reference's
+// convolution example), opted in to the GB300 rgb8 path.
+struct pixel3 {
+	std::uint8_t r, g, b;
+};
+struct pixel3_sum {
+	double r, g, b;
+	IANE_DECL_HYBRID pixel3_sum operator+(pixel3_sum o) const { return {r + o.r, g + o.g, b + o.b}; }
+	IANE_DECL_HYBRID static std::uint8_t byte(double v)
+	{
+		if (!(v > 0.0)) return 0;
+		if (v >= 255.0) return 255;
+		const auto w = static_cast<unsigned int>(v);
+		return static_cast<std::uint8_t>(w + (v - w >= 0.5));
+	}
+	IANE_DECL_HYBRID explicit operator pixel3() const { return {byte(r), byte(g), byte(b)}; }
+};
+IANE_DECL_HYBRID inline pixel3_sum operator*(pixel3 p, float k)
+{
+	const double d = k;
+	return {p.r * d, p.g * d, p.b * d};
+}
+template<>
+struct iane::gb::packed_rgb8<pixel3> : std::true_type {};
+
 namespace {
 
 using dev_src = iane::const_device_image_view<float, 3>;
@@ -29,6 +54,11 @@ static_assert(std::is_same_v<decltype(iane::convolve(std::declval<dev_src>(), st
 	std::declval<dev_dst>())), iane::gb::execution>);
 static_assert(std::is_same_v<decltype(iane::convolve(std::declval<dev_src8>(), std::declval<dev_k2>(),
 	std::declval<dev_dst8>(), iane::convolution_options{}, iane::cuda_policy{})), iane::gb::execution>);
+// ... so do opted-in rgb8 pixels, and texture sources with memory kernels and destinations ...
+static_assert(std::is_same_v<decltype(iane::convolve(std::declval<iane::const_device_image_view<pixel3, 2>>(),
+	std::declval<dev_k2>(), std::declval<iane::device_image_view<pixel3, 2>>())), iane::gb::execution>);
+static_assert(std::is_same_v<decltype(iane::convolve(std::declval<iane::texture_image_view<std::uint8_t, 2>>(),
+	std::declval<dev_k2>(), std::declval<dev_dst8>())), iane::gb::execution>);
 // ... host views keep the reference's template.
 static_assert(!std::is_same_v<decltype(iane::convolve(std::declval<host_src>(), std::declval<host_src>(),
 	std::declval<host_dst>())), iane::gb::execution>);
@@ -101,6 +131,31 @@ int main()
 		}
 	}
 	std::printf("ok   FFT convolution matches the reference\n");
+	{
+		// a texture source: the reference's own texture test shape
+		// (test/unit/algorithms/test_convolution_cuda.cu:53-86) against its CPU convolution
+		iane::host_image<float, 2> source(iane::math::vec2i{5, 4}), kernel(iane::math::vec2i{3, 3});
+		iane::host_image<float, 2> reference(iane::math::vec2i{3, 3}), output(iane::math::vec2i{3, 3});
+		for (int i = 0; i < 20; ++i) source.pointer()[i] = static_cast<float>(i - 6);
+		for (int i = 0; i < 9; ++i) kernel.pointer()[i] = static_cast<float>(i - 3) / 8.0f;
+		iane::texture_image<float> texture(source.dimensions());
+		iane::device_image<float, 2> device_kernel(kernel.dimensions()), device_output(iane::math::vec2i{3, 3});
+		iane::copy(source.const_view(), texture).wait();
+		iane::copy(kernel.const_view(), device_kernel.view()).wait();
+		const iane::math::vec2i origin{1, 1}, crop{3, 3};
+		iane::convolve(source.const_view().subview(origin, crop), kernel.const_view(), reference.view(),
+			{.border = iane::border_mode::clamp});
+		iane::convolve(texture.const_view().subview(origin, crop), device_kernel.const_view(), device_output.view(),
+			{.border = iane::border_mode::clamp}).wait();
+		iane::copy(device_output.const_view(), output.view()).wait();
+		for (int i = 0; i < 9; ++i) {
+			if (output.pointer()[i] != reference.pointer()[i]) {
+				std::printf("FAIL texture convolution differs at %d\n", i);
+				return 1;
+			}
+		}
+		std::printf("ok   texture convolution matches the reference\n");
+	}
 	auto exec = iane::make_execution_context(iane::cuda_policy{});
 	auto op = exec.prepare(iane::gb::richardson_lucy{d_k.const_view(), 5, 1e-6f, iane::gb::rl_start::mean},
 		d_src.const_view(), d_out.view());
