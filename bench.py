@@ -487,6 +487,51 @@ def measure_reference_benchmark_leg(dev, stream, cpu=True, reps=20):
     return out
 
 
+def measure_wiener_leg(dev, stream, cpu=True, reps=20):
+    """Wiener deconvolution (the reference's examples/wiener/main.cu:44-83) of a 2560x1920 u8
+    image (the reference benchmark's pattern) with a 9x9 Gaussian PSF (sigma 2), noise 0.002,
+    u8 output: device time per prepared run (CUDA events; R2C, filter, C2R and the u8
+    encode), and the numpy restatement (float64 DFTs, one host thread) as the CPU baseline."""
+    import numpy as np
+    import torch
+
+    import iane_gb300
+    from iane_gb300 import synth
+
+    width, height = 2560, 1920
+    i = np.arange(width * height, dtype=np.int64)
+    image = (((i * 19) ^ (i // width)) & 0xFF).astype(np.uint8).reshape(height, width)
+    psf_np = synth.gaussian_psf((9, 9), (2.0, 2.0))
+    obs = torch.from_numpy(image).to(dev)
+    out = torch.empty_like(obs)
+    w = iane_gb300.Wiener(torch.from_numpy(psf_np).to(dev), image.shape, 0.002, stream=stream)
+    scratch = torch.empty(w.scratch_bytes, dtype=torch.uint8, device=dev)
+    for _ in range(3):
+        w.run(obs, out, scratch=scratch, stream=stream)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        w.run(obs, out, scratch=scratch, stream=stream)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / reps
+    leg = {"ms": ms, "gpixel_s": image.size / (ms / 1e3) / 1e9,
+           "config": "2560x1920 u8, 9x9 Gaussian PSF sigma 2, noise 0.002, u8 output"}
+    if cpu:
+        import oracle
+
+        t0 = time.perf_counter()
+        ref = oracle.wiener(image, psf_np, 0.002)
+        cms = (time.perf_counter() - t0) * 1e3
+        diff = np.abs(out.cpu().numpy().astype(np.int32) - ref.astype(np.int32))
+        leg["cpu_baseline"] = {"ms": cms, "cores": 1, "kind": "port", "sample": "1 full image (numpy float64 FFT)"}
+        leg["max_level_difference_vs_oracle"] = int(diff.max())
+        leg["gpu_speedup_vs_cpu"] = cms / ms
+    w.close()
+    return leg
+
+
 def measure_learned_leg(dev):
     """Learned warm start: the shipped network's start + BF16 tensor-core RL against plain FP32
     RL from the flat start on the 256x256x64 ellipsoid volume (200 ellipsoids), isotropic
@@ -599,6 +644,7 @@ def main():
     learned_leg = measure_learned_leg(dev)
     fft_leg = measure_fft_leg(dev, stream)
     reference_benchmark_leg = measure_reference_benchmark_leg(dev, stream, cpu=with_cpu)
+    wiener_leg = measure_wiener_leg(dev, stream, cpu=with_cpu)
 
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
@@ -660,6 +706,7 @@ def main():
             "learned_warm_start_leg": learned_leg,
             "fft_leg": fft_leg,
             "reference_benchmark_leg": reference_benchmark_leg,
+            "wiener_leg": wiener_leg,
         }
         print(json.dumps(line), flush=True)
     rl.close()

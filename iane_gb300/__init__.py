@@ -9,6 +9,7 @@ supplies device memory and streams only; every computation runs in ``libiane_gb3
 * :func:`convolve_separable` -- the same with an outer-product kernel, one fused pass.
 * :func:`convolve_rgb8` -- packed (r, g, b) byte pixels, each channel summed on its own: the
   custom element of the reference's convolution example (examples/convolution/main.cu:20-56).
+* :class:`Wiener` -- prepared Wiener deconvolution (examples/wiener/main.cu:44-83).
 * :class:`Texture` / :class:`TextureView` -- the reference's texture_image and
   texture_image_view (include/iane/resource/cuda/texture_image.hpp,
   include/iane/view/texture_image_view.hpp); a :class:`TextureView` is a valid ``src`` of
@@ -28,7 +29,7 @@ from . import abi
 from ._lib import IaneError, IaneInvalidArgument, IaneLengthError, check, lib
 
 __all__ = [
-    "abi", "convolve", "convolve_separable", "convolve_rgb8", "Texture", "TextureView", "RichardsonLucy",
+    "abi", "convolve", "convolve_separable", "convolve_rgb8", "Texture", "TextureView", "Wiener", "RichardsonLucy",
     "RichardsonLucyBatch", "device_status", "IaneError", "IaneInvalidArgument", "IaneLengthError",
 ]
 
@@ -95,6 +96,45 @@ def convolve_rgb8(src, kernel, dst, border="clamp", exact: bool = False, stream=
     check(lib().iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), _border(border), flags,
                                  _stream_handle(stream)))
     return dst
+
+
+class Wiener:
+    """Prepared Wiener deconvolution (the reference's examples/wiener/main.cu:44-83): the
+    PSF (f32 CUDA tensor of the image rank, centred at the origin with periodic wrap-around)
+    becomes the filter conj(H) / (|H|^2 + noise) once; ``run`` restores an observed image of
+    ``shape`` into ``restored`` (uint8: the example's to_gray8; float32: the plain value)."""
+
+    def __init__(self, psf, shape, noise: float = 0.002, stream=None):
+        self.shape = tuple(int(n) for n in shape)
+        rank = len(self.shape)
+        k = _device_view(psf)
+        ext = (ctypes.c_int32 * 3)(*([self.shape[rank - 1 - i] for i in range(rank)] + [1] * (3 - rank)))
+        handle = ctypes.c_void_p()
+        check(lib().iane_gb_wiener_prepare(ctypes.byref(k), rank, ext, float(noise), _stream_handle(stream),
+                                           ctypes.byref(handle)))
+        self._plan = handle
+        self.scratch_bytes = int(lib().iane_gb_wiener_scratch_bytes(handle))
+
+    def run(self, observed, restored, scratch=None, stream=None):
+        import torch
+
+        if scratch is None:
+            scratch = torch.empty(self.scratch_bytes, dtype=torch.uint8, device=observed.device)
+        s, d = _device_view(observed), _device_view(restored)
+        check(lib().iane_gb_wiener_run(self._plan, ctypes.byref(s), ctypes.byref(d), scratch.data_ptr(),
+                                       scratch.numel(), _stream_handle(stream)))
+        return restored
+
+    def close(self) -> None:
+        if getattr(self, "_plan", None):
+            lib().iane_gb_wiener_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Texture:

@@ -112,6 +112,13 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_texture_upload.argtypes = [u64, _VIEW_P, vp]
     l.iane_gb_texture_destroy.argtypes = [u64]
     l.iane_gb_convolve_texture.argtypes = [ctypes.POINTER(abi.TextureView), _VIEW_P, _VIEW_P, i, ctypes.c_uint, vp]
+    l.iane_gb_wiener_prepare.argtypes = [_VIEW_P, i, i32p, f, vp, ctypes.POINTER(vp)]
+    l.iane_gb_wiener_scratch_bytes.argtypes = [cvp]
+    l.iane_gb_wiener_scratch_bytes.restype = sz
+    l.iane_gb_wiener_run.argtypes = [vp, _VIEW_P, _VIEW_P, vp, sz, vp]
+    l.iane_gb_wiener_destroy.argtypes = [vp]
+    for name in ("wiener_prepare", "wiener_run", "wiener_destroy"):
+        getattr(l, "iane_gb_" + name).restype = ctypes.c_int
     for name in ("texture_create", "texture_upload", "texture_destroy", "convolve_texture"):
         getattr(l, "iane_gb_" + name).restype = ctypes.c_int
     if l.iane_gb_abi_version() != abi.ABI_VERSION:

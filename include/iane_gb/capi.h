@@ -230,6 +230,26 @@ int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int ob
 int iane_gb_rl_destroy(iane_gb_rl_plan* plan);
 
 /*
+ * Wiener deconvolution, prepared (the reference's examples/wiener/main.cu:44-83, 2-D there;
+ * rank 1-3 here). prepare: `psf` is an f32 device view of the image's rank and no larger than
+ * `extent` on any axis (the example normalises it to sum one first; it is used as given
+ * here); it is centred at the origin with periodic wrap-around, transformed, and turned into
+ * the filter conj(H) / (|H|^2 + noise); noise must be finite and positive. Synchronous.
+ * run: restored = IFFT(FFT(observed) * filter) / N, periodic boundary, FP32 transforms;
+ * observed is any scalar view except f64, restored u8 (the example's to_gray8: round half
+ * up, saturate) or another scalar type (the reference's casts from the FP32 value).
+ * `scratch` (device, >= iane_gb_wiener_scratch_bytes) holds the buffers and the FFT work
+ * area. A plan runs on one stream at a time.
+ */
+typedef struct iane_gb_wiener_plan iane_gb_wiener_plan;
+int iane_gb_wiener_prepare(const iane_gb_view* psf, int rank, const int32_t* extent, float noise, void* stream,
+	iane_gb_wiener_plan** plan);
+size_t iane_gb_wiener_scratch_bytes(const iane_gb_wiener_plan* plan);
+int iane_gb_wiener_run(iane_gb_wiener_plan* plan, const iane_gb_view* observed, const iane_gb_view* restored,
+	void* scratch, size_t scratch_bytes, void* stream);
+int iane_gb_wiener_destroy(iane_gb_wiener_plan* plan);
+
+/*
  * Batched Richardson-Lucy over many 2-D images of uneven size, each with its own PSF. No
  * counterpart in the reference (its example runs one image per process). Each pass of every
  * iteration is one persistent launch per tile shape over a device work queue of

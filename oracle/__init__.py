@@ -7,6 +7,11 @@ always as the checker or the timed CPU baseline, never as the product. It loads
 * ``_ref/libiane_ref.so`` (where it was built): the reference's own ``iane::convolve`` and a
   restated ``prepare_rl`` built from the reference's views and algorithms.
 
+``wiener`` is a numpy restatement: the reference's Wiener example runs on FFTW (CPU) or
+cuFFT, and FFTW is not installed here, so the oracle uses float64 DFTs (numpy's FFT),
+pinned by tests to the direct DFT definition the reference's own FFT tests check
+(test/unit/prepared/real_fft_cases.hpp:47-75) and to closed-form answers.
+
 Arrays are C-ordered numpy arrays (slowest axis first); see ``iane_gb300.abi`` for the
 mapping to IANE's axis-0-fastest views.
 """
@@ -191,3 +196,34 @@ def mirror_pad(src: np.ndarray, radii) -> np.ndarray:
         idx = np.where(m < n, m, 2 * n - 1 - m)
         out = np.take(out, idx, axis=axis)
     return np.ascontiguousarray(out)
+
+
+def wiener_pad_psf(psf: np.ndarray, shape) -> np.ndarray:
+    """The PSF in an image-sized buffer with its centre (extent // 2 per axis) at the origin,
+    wrapped periodically (examples/wiener/main.cu:112-120)."""
+    pad = np.zeros(shape, np.float64)
+    pad[tuple(slice(0, e) for e in psf.shape)] = psf
+    return np.roll(pad, [-(e // 2) for e in psf.shape], axis=tuple(range(psf.ndim)))
+
+
+def to_gray8(values: np.ndarray) -> np.ndarray:
+    """examples/common/deconvolution.hpp:43-55 on float32 values: round half up, saturate."""
+    v = values.astype(np.float32)
+    out = np.zeros(v.shape, np.uint8)
+    inside = (v > 0) & (v < 255)
+    whole = np.floor(v[inside])
+    out[inside] = (whole + ((v[inside] - whole) >= np.float32(0.5))).astype(np.uint8)
+    out[v >= 255] = 255
+    return out
+
+
+def wiener(observed: np.ndarray, psf: np.ndarray, noise: float, out_dtype=np.uint8) -> np.ndarray:
+    """Wiener deconvolution (examples/wiener/main.cu:44-83): IFFT(FFT(observed) * conj(H) /
+    (|H|^2 + noise)) / N with H the spectrum of the wrapped PSF; u8 output through to_gray8,
+    float32 output as the value."""
+    h = np.fft.fftn(wiener_pad_psf(psf.astype(np.float64), observed.shape))
+    o = np.fft.fftn(observed.astype(np.float64))
+    r = np.fft.ifftn(o * np.conj(h) / (h.real ** 2 + h.imag ** 2 + float(np.float32(noise)))).real
+    if np.dtype(out_dtype) == np.uint8:
+        return to_gray8(r)
+    return r.astype(out_dtype)

@@ -188,3 +188,43 @@ def test_oracle_rl_matches_live_reference_with_u8_like_data():
         a = oracle.rl(obs, psf, 6, 1e-6, init=init)
         b = oracle.rl(obs, psf, 6, 1e-6, init=init, use_reference=True)
         assert np.array_equal(a, b)
+
+
+# --- Wiener (numpy restatement) -------------------------------------------------------------
+
+def test_wiener_oracle_dft_matches_direct_definition():
+    # the reference's FFT test computes each bin as sum x * exp(-2 pi i k x / n) in double
+    # (test/unit/prepared/real_fft_cases.hpp:47-75); the oracle's transform is that sum
+    size = (5, 7)
+    img = ((np.arange(35) * 7) % 11 - 4).astype(np.float64).reshape(size)
+    spec = np.fft.fftn(img)
+    ky, kx = np.meshgrid(np.arange(size[0]), np.arange(size[1]), indexing="ij")
+    for v in range(size[0]):
+        for u in range(size[1]):
+            phase = -2 * np.pi * (u * kx / size[1] + v * ky / size[0])
+            direct = np.sum(img * np.cos(phase)) + 1j * np.sum(img * np.sin(phase))
+            assert abs(spec[v, u] - direct) < 3e-5
+
+
+def test_wiener_oracle_known_answers():
+    rng = np.random.default_rng(2)
+    obs = rng.integers(0, 256, (12, 20)).astype(np.uint8)
+    # a centred delta: H = 1, so the result is observed / (1 + noise)
+    delta = np.zeros((3, 5), np.float32)
+    delta[1, 2] = 1.0
+    out = oracle.wiener(obs, delta, 0.25, np.float64)
+    assert np.allclose(out, obs / 1.25, atol=1e-9)
+    assert np.array_equal(oracle.wiener(obs, delta, 0.25), oracle.to_gray8(obs / 1.25))
+    # the PSF centre goes to the origin: an off-centre delta shifts the image back
+    shifted = np.zeros((3, 5), np.float32)
+    shifted[1, 3] = 1.0  # one column right of the centre: convolution shifts by +1 in x
+    out = oracle.wiener(obs, shifted, 1e-9, np.float64)
+    assert np.allclose(out, np.roll(obs, -1, axis=1), atol=1e-6)
+    # the wrapped PSF: tap x lands at (x - e // 2) mod n
+    pad = oracle.wiener_pad_psf(np.arange(15, dtype=np.float32).reshape(3, 5), (4, 6))
+    assert pad[0, 0] == 7 and pad[0, 5] == 6 and pad[3, 4] == 0 and pad[3, 0] == 2 and pad[1, 2] == 14
+
+
+def test_to_gray8_rule():
+    v = np.array([-1.0, 0.0, 0.49, 0.5, 1.5, 2.4999, 254.5, 255.0, 300.0, np.nan], np.float32)
+    assert oracle.to_gray8(v).tolist() == [0, 0, 0, 1, 2, 2, 255, 255, 255, 0]
