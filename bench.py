@@ -532,6 +532,52 @@ def measure_wiener_leg(dev, stream, cpu=True, reps=20):
     return leg
 
 
+def measure_morphology_leg(dev, stream, reps=20):
+    """Flat morphology (include/iane/algorithms/morphology/morphology.hpp): erosion of the
+    2560x1920 u8 benchmark image with a 5x5 box, and erosion and opening of a 512^3 f32 volume
+    with a 5x5x5 box, zero border. Device time per call (CUDA events) and the algorithmic
+    bandwidth (each pass reads and writes the image once; the 3-D box runs as an xy pass and a z
+    pass, so 4 image transfers per erosion) against the measured HBM peak."""
+    import numpy as np
+    import torch
+
+    import iane_gb300
+
+    peak = measured_peaks()[0].get("hbm_gbs") or 6800.0
+    out = {}
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / reps
+
+    width, height = 2560, 1920
+    i = np.arange(width * height, dtype=np.int64)
+    img = torch.from_numpy((((i * 19) ^ (i // width)) & 0xFF).astype(np.uint8).reshape(height, width)).to(dev)
+    dst = torch.empty_like(img)
+    ms = timed(lambda: iane_gb300.morphology(img, dst, (2, 2), "erode", "zero", stream=stream))
+    out["erode_u8_2560x1920_box5"] = {"ms": ms, "gbs": 2 * img.numel() / (ms / 1e3) / 1e9}
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    vol = torch.rand((512, 512, 512), generator=gen, device=dev)
+    vdst = torch.empty_like(vol)
+    scratch = torch.empty(2 * vol.numel() * 4 + 1024, dtype=torch.uint8, device=dev)
+    ms = timed(lambda: iane_gb300.morphology(vol, vdst, (2, 2, 2), "erode", "zero", stream=stream))
+    gbs = 4 * vol.numel() * 4 / (ms / 1e3) / 1e9
+    out["erode_f32_512cubed_box5"] = {"ms": ms, "gbs": gbs, "hbm_frac": gbs / peak}
+    ms = timed(lambda: iane_gb300.morphology(vol, vdst, (2, 2, 2), "opening", "zero", scratch=scratch, stream=stream))
+    gbs = 8 * vol.numel() * 4 / (ms / 1e3) / 1e9
+    out["opening_f32_512cubed_box5"] = {"ms": ms, "gbs": gbs, "hbm_frac": gbs / peak}
+    return out
+
+
 def measure_learned_leg(dev):
     """Learned warm start: the shipped network's start + BF16 tensor-core RL against plain FP32
     RL from the flat start on the 256x256x64 ellipsoid volume (200 ellipsoids), isotropic
@@ -645,6 +691,7 @@ def main():
     fft_leg = measure_fft_leg(dev, stream)
     reference_benchmark_leg = measure_reference_benchmark_leg(dev, stream, cpu=with_cpu)
     wiener_leg = measure_wiener_leg(dev, stream, cpu=with_cpu)
+    morphology_leg = measure_morphology_leg(dev, stream)
 
     # result sanity: the run converged to something finite and positive
     est_np = est.cpu().numpy()
@@ -707,6 +754,7 @@ def main():
             "fft_leg": fft_leg,
             "reference_benchmark_leg": reference_benchmark_leg,
             "wiener_leg": wiener_leg,
+            "morphology_leg": morphology_leg,
         }
         print(json.dumps(line), flush=True)
     rl.close()

@@ -10,6 +10,8 @@ supplies device memory and streams only; every computation runs in ``libiane_gb3
 * :func:`convolve_rgb8` -- packed (r, g, b) byte pixels, each channel summed on its own: the
   custom element of the reference's convolution example (examples/convolution/main.cu:20-56).
 * :class:`Wiener` -- prepared Wiener deconvolution (examples/wiener/main.cu:44-83).
+* :func:`morphology` -- flat erosion, dilation, opening and closing
+  (include/iane/algorithms/morphology/morphology.hpp).
 * :class:`Texture` / :class:`TextureView` -- the reference's texture_image and
   texture_image_view (include/iane/resource/cuda/texture_image.hpp,
   include/iane/view/texture_image_view.hpp); a :class:`TextureView` is a valid ``src`` of
@@ -29,7 +31,8 @@ from . import abi
 from ._lib import IaneError, IaneInvalidArgument, IaneLengthError, check, lib
 
 __all__ = [
-    "abi", "convolve", "convolve_separable", "convolve_rgb8", "Texture", "TextureView", "Wiener", "RichardsonLucy",
+    "abi", "convolve", "convolve_separable", "convolve_rgb8", "morphology", "Texture", "TextureView", "Wiener",
+    "RichardsonLucy",
     "RichardsonLucyBatch", "device_status", "IaneError", "IaneInvalidArgument", "IaneLengthError",
 ]
 
@@ -95,6 +98,42 @@ def convolve_rgb8(src, kernel, dst, border="clamp", exact: bool = False, stream=
     flags = abi.ACC_EXACT if exact else abi.ACC_FAST
     check(lib().iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), _border(border), flags,
                                  _stream_handle(stream)))
+    return dst
+
+
+def morphology(src, dst, radius, op: str = "erode", border="clamp", footprint=None, scratch=None, stream=None):
+    """Flat morphology (include/iane/algorithms/morphology/morphology.hpp): ``op`` is
+    "erode", "dilate", "opening" or "closing"; ``radius`` is C-ordered like the tensors;
+    ``footprint`` is None (the whole box) or a CUDA uint8/bool tensor of shape 2 * radius + 1
+    whose nonzero cells are contained. Opening and closing run through ``scratch`` (allocated
+    when None) and may run in place (``src is dst``); erode and dilate need disjoint views."""
+    if op not in abi.MORPHOLOGY_OPS:
+        raise ValueError(f"unknown morphology op {op!r}")
+    s, d = _device_view(src), _device_view(dst)
+    rank = len(src.shape)
+    radius = tuple(int(r) for r in radius)
+    if len(radius) != rank:
+        raise ValueError("radius needs one entry per axis")
+    r = (ctypes.c_int32 * 3)(*([radius[rank - 1 - i] for i in range(rank)] + [0] * (3 - rank)))
+    mask = None
+    if footprint is not None:
+        if tuple(footprint.shape) != tuple(2 * v + 1 for v in radius) or not footprint.is_cuda:
+            raise ValueError("footprint must be a CUDA tensor of shape 2 * radius + 1")
+        mask = footprint.contiguous().to(dtype=__import__("torch").uint8)
+    code = abi.MORPHOLOGY_OPS[op]
+    mp = None if mask is None else mask.data_ptr()
+    if code in (abi.ERODE, abi.DILATE):
+        check(lib().iane_gb_morphology(ctypes.byref(s), ctypes.byref(d), r, mp, code, _border(border),
+                                       _stream_handle(stream)))
+        return dst
+    ext = (ctypes.c_int32 * 3)(*[s.extent[i] for i in range(3)])
+    need = int(lib().iane_gb_morphology_scratch_bytes(s.dtype, rank, ext))
+    if scratch is None:
+        import torch
+
+        scratch = torch.empty(max(need, 1), dtype=torch.uint8, device=src.device)
+    check(lib().iane_gb_morphology_compound(ctypes.byref(s), ctypes.byref(d), r, mp, code, _border(border),
+                                            scratch.data_ptr(), scratch.numel(), _stream_handle(stream)))
     return dst
 
 

@@ -112,6 +112,13 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_texture_upload.argtypes = [u64, _VIEW_P, vp]
     l.iane_gb_texture_destroy.argtypes = [u64]
     l.iane_gb_convolve_texture.argtypes = [ctypes.POINTER(abi.TextureView), _VIEW_P, _VIEW_P, i, ctypes.c_uint, vp]
+    u8p = ctypes.c_void_p
+    l.iane_gb_morphology.argtypes = [_VIEW_P, _VIEW_P, i32p, u8p, i, i, vp]
+    l.iane_gb_morphology.restype = ctypes.c_int
+    l.iane_gb_morphology_scratch_bytes.argtypes = [i, i, i32p]
+    l.iane_gb_morphology_scratch_bytes.restype = sz
+    l.iane_gb_morphology_compound.argtypes = [_VIEW_P, _VIEW_P, i32p, u8p, i, i, vp, sz, vp]
+    l.iane_gb_morphology_compound.restype = ctypes.c_int
     l.iane_gb_wiener_prepare.argtypes = [_VIEW_P, i, i32p, f, vp, ctypes.POINTER(vp)]
     l.iane_gb_wiener_scratch_bytes.argtypes = [cvp]
     l.iane_gb_wiener_scratch_bytes.restype = sz

@@ -24,6 +24,8 @@ ACC_FAST, ACC_EXACT = 0, 1
 CONV_FFT, CONV_AUTO = 2, 4
 
 RL_INIT_OBSERVED, RL_INIT_MEAN, RL_INIT_GIVEN = 0, 1, 2
+ERODE, DILATE, OPENING, CLOSING = 0, 1, 2, 3
+MORPHOLOGY_OPS = {"erode": ERODE, "dilate": DILATE, "opening": OPENING, "closing": CLOSING}
 RL_BF16_TENSOR = 1
 BATCH_AUTOTUNE = 1
 

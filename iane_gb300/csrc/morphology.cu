@@ -1,0 +1,323 @@
+// Flat morphology: erosion, dilation and the prepared opening / closing of the reference's
+// include/iane/algorithms/morphology/morphology.hpp (rank 1-3 here).
+//
+// erode(p)  = min over footprint offsets o of sample(p + o)
+// dilate(p) = max over footprint offsets o of sample(p - o)
+// with o = position - radius for positions in [0, 2 r] in raster order (axis 0 fastest), the
+// border rule applied per axis (a zero-border sample is the value 0 and takes part), and the
+// reference's update rule `value < result` (`>` for dilation) starting from +inf / -inf (the
+// type's max / lowest for integers): NaN never replaces the running value, an all-NaN
+// neighbourhood stays at the start value, and among equal values (-0 and +0) the first in
+// scan order wins (morphology.hpp:44-71).
+//
+// Box footprints run separably -- one kernel scans x then y in shared memory per plane, a
+// second scans z -- in the same order per axis as the reference's raster scan (reversed for
+// dilation, whose samples run p + r down to p - r). The first extreme of the raster scan is
+// the first extreme along z of the first along y of the first along x, so the separable
+// result is bit-identical, signed zeros included. Masked footprints (any subset of the box)
+// take the direct kernel, which scans the footprint in raster order.
+#include "common.cuh"
+#include "kernels.h"
+
+#include <limits>
+#include <string>
+#include <type_traits>
+
+namespace iane_gb {
+namespace {
+
+constexpr int kTX = 32;  // box kernel: outputs per block along x
+constexpr int kTY = 32;  //             and along y (8 rows of threads, 4 outputs each)
+
+template<class T> __device__ __forceinline__ T start_value(bool dilate)
+{
+	if constexpr (std::is_floating_point_v<T>) {
+		return dilate ? -std::numeric_limits<T>::infinity() : std::numeric_limits<T>::infinity();
+	} else {
+		return dilate ? std::numeric_limits<T>::lowest() : std::numeric_limits<T>::max();
+	}
+}
+
+template<bool DILATE, class T> __device__ __forceinline__ void take(T v, T& r)
+{
+	if (DILATE ? v > r : v < r) r = v;
+}
+
+template<class T> __device__ __forceinline__ T sample(const DevView& v, int x, int y, int z, int border)
+{
+	int xi = 0, yi = 0, zi = 0;
+	if (map_coord(x, v.ext[0], border, xi) && map_coord(y, v.ext[1], border, yi) && map_coord(z, v.ext[2], border, zi)) {
+		return *element_ptr<T>(v, xi, yi, zi);
+	}
+	return T(0);
+}
+
+// Box footprint, x then y, for one 32x32 output tile of plane blockIdx.z. Shared memory: the
+// (32 + 2 rx) x (32 + 2 ry) input tile, then the 32 x (32 + 2 ry) x-pass results.
+template<class T, bool DILATE>
+__global__ void __launch_bounds__(256) morph_box_xy_kernel(DevView src, DevView dst, int rx, int ry, int border)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const int tw = kTX + 2 * rx, th = kTY + 2 * ry;
+	T* tile = reinterpret_cast<T*>(smem_raw);
+	T* xbuf = tile + tw * th;
+	const int tid = threadIdx.y * 32 + threadIdx.x;
+	const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z = blockIdx.z;
+	for (int i = tid; i < tw * th; i += 256) {
+		const int r = i / tw, c = i - r * tw;
+		tile[i] = sample<T>(src, x0 - rx + c, y0 - ry + r, z, border);
+	}
+	__syncthreads();
+	for (int i = tid; i < kTX * th; i += 256) {
+		const int r = i / kTX, c = i - r * kTX;
+		T m = start_value<T>(DILATE);
+		const T* row = tile + r * tw + c;
+		for (int o = 0; o <= 2 * rx; ++o) take<DILATE>(row[DILATE ? 2 * rx - o : o], m);
+		xbuf[i] = m;
+	}
+	__syncthreads();
+	const int x = x0 + threadIdx.x;
+	if (x >= dst.ext[0]) return;
+	for (int k = 0; k < kTY / 8; ++k) {
+		const int r = threadIdx.y + 8 * k;
+		const int y = y0 + r;
+		if (y >= dst.ext[1]) break;
+		T m = start_value<T>(DILATE);
+		for (int o = 0; o <= 2 * ry; ++o) take<DILATE>(xbuf[(r + (DILATE ? 2 * ry - o : o)) * kTX + threadIdx.x], m);
+		*const_cast<T*>(element_ptr<T>(dst, x, y, z)) = m;
+	}
+}
+
+// Box footprint along z (after the xy pass): one output per thread.
+template<class T, bool DILATE>
+__global__ void __launch_bounds__(256) morph_box_z_kernel(DevView src, DevView dst, int rz, int border)
+{
+	const int x = blockIdx.x * 32 + threadIdx.x;
+	const int y = blockIdx.y * 8 + threadIdx.y;
+	const int z = blockIdx.z;
+	if (x >= dst.ext[0] || y >= dst.ext[1]) return;
+	T m = start_value<T>(DILATE);
+	for (int o = 0; o <= 2 * rz; ++o) {
+		int zi = 0;
+		const int zs = DILATE ? z + rz - o : z - rz + o;
+		const T v = map_coord(zs, src.ext[2], border, zi) ? *element_ptr<T>(src, x, y, zi) : T(0);
+		take<DILATE>(v, m);
+	}
+	*const_cast<T*>(element_ptr<T>(dst, x, y, z)) = m;
+}
+
+// Any flat footprint (mask of (2r+1) per axis, raster order, nonzero = contained): one output
+// per thread, the footprint scanned in raster order.
+template<class T, bool DILATE>
+__global__ void __launch_bounds__(256) morph_direct_kernel(DevView src, DevView dst, int rx, int ry, int rz,
+	const uint8_t* __restrict__ mask, int border)
+{
+	const int x = blockIdx.x * 32 + threadIdx.x;
+	const int y = blockIdx.y * 8 + threadIdx.y;
+	const int z = blockIdx.z;
+	if (x >= dst.ext[0] || y >= dst.ext[1]) return;
+	T m = start_value<T>(DILATE);
+	int q = 0;
+	for (int pz = 0; pz <= 2 * rz; ++pz) {
+		for (int py = 0; py <= 2 * ry; ++py) {
+			for (int px = 0; px <= 2 * rx; ++px, ++q) {
+				if (mask && !mask[q]) continue;
+				const int ox = px - rx, oy = py - ry, oz = pz - rz;
+				const T v = DILATE ? sample<T>(src, x - ox, y - oy, z - oz, border) : sample<T>(src, x + ox, y + oy, z + oz, border);
+				take<DILATE>(v, m);
+			}
+		}
+	}
+	*const_cast<T*>(element_ptr<T>(dst, x, y, z)) = m;
+}
+
+size_t box_xy_smem(int rx, int ry, int esize)
+{
+	return static_cast<size_t>((kTX + 2 * rx) * (kTY + 2 * ry) + kTX * (kTY + 2 * ry)) * esize;
+}
+
+template<class T, bool DILATE>
+int launch_op(const DevView& s, const DevView& d, const int* r, const uint8_t* mask, int border, void* temp,
+	cudaStream_t st)
+{
+	const dim3 g8((d.ext[0] + 31) / 32, (d.ext[1] + 7) / 8, d.ext[2]);
+	if (mask) {
+		morph_direct_kernel<T, DILATE><<<g8, dim3(32, 8), 0, st>>>(s, d, r[0], r[1], r[2], mask, border);
+		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
+		return IANE_GB_OK;
+	}
+	const size_t smem = box_xy_smem(r[0], r[1], sizeof(T));
+	if (smem > 200 * 1024) {
+		morph_direct_kernel<T, DILATE><<<g8, dim3(32, 8), 0, st>>>(s, d, r[0], r[1], r[2], nullptr, border);
+		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
+		return IANE_GB_OK;
+	}
+	auto xy = morph_box_xy_kernel<T, DILATE>;
+	IANE_GB_CUDA(cudaFuncSetAttribute(xy, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+		"morphology: shared memory");
+	const dim3 gt((d.ext[0] + kTX - 1) / kTX, (d.ext[1] + kTY - 1) / kTY, d.ext[2]);
+	if (r[2] == 0) {
+		xy<<<gt, dim3(32, 8), smem, st>>>(s, d, r[0], r[1], border);
+		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
+		return IANE_GB_OK;
+	}
+	// 3-D box: xy into a packed temporary, then z into the destination
+	DevView t{};
+	t.ptr = static_cast<char*>(temp);
+	t.dtype = d.dtype;
+	t.rank = d.rank;
+	for (int i = 0; i < 3; ++i) t.ext[i] = d.ext[i];
+	t.stride[0] = sizeof(T);
+	t.stride[1] = t.stride[0] * t.ext[0];
+	t.stride[2] = t.stride[1] * t.ext[1];
+	xy<<<gt, dim3(32, 8), smem, st>>>(s, t, r[0], r[1], border);
+	morph_box_z_kernel<T, DILATE><<<g8, dim3(32, 8), 0, st>>>(t, d, r[2], border);
+	IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
+	return IANE_GB_OK;
+}
+
+template<class T>
+int launch_typed(const DevView& s, const DevView& d, const int* r, const uint8_t* mask, int op, int border,
+	void* temp, cudaStream_t st)
+{
+	return op == IANE_GB_DILATE ? launch_op<T, true>(s, d, r, mask, border, temp, st)
+		: launch_op<T, false>(s, d, r, mask, border, temp, st);
+}
+
+int launch_any(const DevView& s, const DevView& d, const int* r, const uint8_t* mask, int op, int border, void* temp,
+	cudaStream_t st)
+{
+	switch (s.dtype) {
+	case IANE_GB_U8: return launch_typed<uint8_t>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_I8: return launch_typed<int8_t>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_U16: return launch_typed<uint16_t>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_I16: return launch_typed<int16_t>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_I32: return launch_typed<int32_t>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_U32: return launch_typed<uint32_t>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_F32: return launch_typed<float>(s, d, r, mask, op, border, temp, st);
+	case IANE_GB_F64: return launch_typed<double>(s, d, r, mask, op, border, temp, st);
+	default: return fail(IANE_GB_UNSUPPORTED, "morphology: element type (u8, i8, u16, i16, i32, u32, f32, f64)");
+	}
+}
+
+// Shared argument checks; fills r[3] (unused axes 0).
+int check_args(const iane_gb_view* src, const iane_gb_view* dst, const int32_t* radius, int border, DevView& s,
+	DevView& d, int r[3])
+{
+	int status = normalise_view(src, "morphology source", &s);
+	if (status) return status;
+	status = normalise_view(dst, "morphology destination", &d);
+	if (status) return status;
+	if (!radius) return fail(IANE_GB_INVALID_ARGUMENT, "morphology: null radius");
+	if (s.rank != d.rank) return fail(IANE_GB_INVALID_ARGUMENT, "morphology: source and destination need the same rank");
+	if (s.dtype != d.dtype) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "morphology: source and destination need the same element type");
+	}
+	for (int i = 0; i < 3; ++i) {
+		if (s.ext[i] != d.ext[i]) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "Source and destination require matching nonnegative dimensions");
+		}
+		r[i] = i < s.rank ? radius[i] : 0;
+		// morphology.hpp:76-88
+		if (r[i] < 0 || r[i] > 1 << 14) {
+			return fail(IANE_GB_INVALID_ARGUMENT, "Morphology requires a nonnegative radius with representable width");
+		}
+	}
+	if (border < IANE_GB_BORDER_CLAMP || border > IANE_GB_BORDER_MIRROR) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "morphology: unknown border mode");
+	}
+	if (s.ext[1] > 65535 * 8 || s.ext[2] > 65535) {
+		return fail(IANE_GB_UNSUPPORTED, "morphology: image too large along axis 1 or 2 for the grid");
+	}
+	return IANE_GB_OK;
+}
+
+// The direct kernel scans the whole footprint per output: bound its work.
+int check_direct(const int r[3], const uint8_t* mask, int esize)
+{
+	const bool direct = mask || box_xy_smem(r[0], r[1], esize) > 200 * 1024;
+	const long long cells = static_cast<long long>(2 * r[0] + 1) * (2 * r[1] + 1) * (2 * r[2] + 1);
+	if (direct && cells > (1LL << 20)) {
+		return fail(IANE_GB_UNSUPPORTED, "morphology: footprint too large for the direct kernel (over 2^20 cells)");
+	}
+	return IANE_GB_OK;
+}
+
+size_t packed_bytes(const DevView& d)
+{
+	return (static_cast<size_t>(element_count(d)) * dtype_size(d.dtype) + 255) & ~size_t(255);
+}
+
+}  // namespace
+}  // namespace iane_gb
+
+using namespace iane_gb;
+
+extern "C" {
+
+int iane_gb_morphology(const iane_gb_view* src, const iane_gb_view* dst, const int32_t* radius,
+	const uint8_t* footprint, int op, int border, void* stream)
+{
+	DevView s{}, d{};
+	int r[3];
+	int status = check_args(src, dst, radius, border, s, d, r);
+	if (status) return status;
+	if (op != IANE_GB_ERODE && op != IANE_GB_DILATE) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "morphology: op must be IANE_GB_ERODE or IANE_GB_DILATE");
+	}
+	if (element_count(s) == 0) return IANE_GB_OK;
+	status = check_direct(r, footprint, dtype_size(d.dtype));
+	if (status) return status;
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	void* temp = nullptr;
+	const bool needs_temp = !footprint && r[2] > 0 && box_xy_smem(r[0], r[1], dtype_size(d.dtype)) <= 200 * 1024;
+	if (needs_temp) {
+		IANE_GB_CUDA(cudaMallocAsync(&temp, packed_bytes(d), st), "morphology: temporary");
+	}
+	status = launch_any(s, d, r, footprint, op, border, temp, st);
+	if (temp) cudaFreeAsync(temp, st);
+	return status;
+}
+
+size_t iane_gb_morphology_scratch_bytes(int dtype, int rank, const int32_t* extent)
+{
+	if (!extent || rank < 1 || rank > 3 || dtype_size(dtype) == 0) return 0;
+	size_t count = 1;
+	for (int i = 0; i < rank; ++i) count *= extent[i] > 0 ? static_cast<size_t>(extent[i]) : 0;
+	// the intermediate image, and the temporary of a 3-D box pass
+	return 2 * ((count * dtype_size(dtype) + 255) & ~size_t(255));
+}
+
+int iane_gb_morphology_compound(const iane_gb_view* src, const iane_gb_view* dst, const int32_t* radius,
+	const uint8_t* footprint, int op, int border, void* scratch, size_t scratch_bytes, void* stream)
+{
+	DevView s{}, d{};
+	int r[3];
+	int status = check_args(src, dst, radius, border, s, d, r);
+	if (status) return status;
+	if (op != IANE_GB_OPENING && op != IANE_GB_CLOSING) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "morphology: op must be IANE_GB_OPENING or IANE_GB_CLOSING");
+	}
+	if (element_count(s) == 0) return IANE_GB_OK;
+	status = check_direct(r, footprint, dtype_size(d.dtype));
+	if (status) return status;
+	const size_t image = packed_bytes(d);
+	if (!scratch || scratch_bytes < 2 * image) {
+		return fail(IANE_GB_LENGTH_ERROR, "morphology: scratch smaller than iane_gb_morphology_scratch_bytes");
+	}
+	// morphology.hpp:118-125: the first pass into a packed intermediate, the second into dst
+	DevView mid = d;
+	mid.ptr = static_cast<char*>(scratch);
+	mid.stride[0] = dtype_size(d.dtype);
+	mid.stride[1] = mid.stride[0] * d.ext[0];
+	mid.stride[2] = mid.stride[1] * d.ext[1];
+	void* temp = static_cast<char*>(scratch) + image;
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	const int first = op == IANE_GB_OPENING ? IANE_GB_ERODE : IANE_GB_DILATE;
+	const int second = op == IANE_GB_OPENING ? IANE_GB_DILATE : IANE_GB_ERODE;
+	status = launch_any(s, mid, r, footprint, first, border, temp, st);
+	if (status) return status;
+	return launch_any(mid, d, r, footprint, second, border, temp, st);
+}
+
+}  // extern "C"

@@ -230,6 +230,31 @@ int iane_gb_rl_run_host(iane_gb_rl_plan* plan, const void* host_observed, int ob
 int iane_gb_rl_destroy(iane_gb_rl_plan* plan);
 
 /*
+ * Flat morphology (the reference's include/iane/algorithms/morphology/morphology.hpp, rank 1-3
+ * here): erode(p) = min over footprint offsets o of src(p + o), dilate(p) = max of src(p - o),
+ * o = position - radius over the (2 radius + 1)-box in raster order, with the border rule
+ * (clamp, zero -- out-of-range samples are the value 0 -- or mirror), NaN ignored (an all-NaN
+ * neighbourhood gives +inf / -inf) and the first of equal values in scan order kept, so
+ * results are bit-identical to the reference's. `footprint` is NULL for the whole box, or a
+ * device mask of prod(2 radius + 1) bytes in raster order (axis 0 fastest, nonzero =
+ * contained; the reference's flat_footprint predicate). src and dst have the same extents and
+ * element type (u8, i8, u16, i16, i32, u32, f32, f64) and do not overlap.
+ */
+#define IANE_GB_ERODE 0
+#define IANE_GB_DILATE 1
+#define IANE_GB_OPENING 2 /* erosion, then dilation (morphology.hpp:216-221) */
+#define IANE_GB_CLOSING 3 /* dilation, then erosion */
+int iane_gb_morphology(const iane_gb_view* src, const iane_gb_view* dst, const int32_t* radius,
+	const uint8_t* footprint, int op, int border, void* stream);
+
+/* Opening or closing through a packed intermediate in `scratch` (device, at least
+ * iane_gb_morphology_scratch_bytes for the image's element type and extents); src and dst may
+ * be the same view (exact in-place execution, as the reference's prepared compound). */
+size_t iane_gb_morphology_scratch_bytes(int dtype, int rank, const int32_t* extent);
+int iane_gb_morphology_compound(const iane_gb_view* src, const iane_gb_view* dst, const int32_t* radius,
+	const uint8_t* footprint, int op, int border, void* scratch, size_t scratch_bytes, void* stream);
+
+/*
  * Wiener deconvolution, prepared (the reference's examples/wiener/main.cu:44-83, 2-D there;
  * rank 1-3 here). prepare: `psf` is an f32 device view of the image's rank and no larger than
  * `extent` on any axis (the example normalises it to sum one first; it is used as given

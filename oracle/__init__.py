@@ -58,6 +58,9 @@ def oracle_lib():
         lib.oracle_rl.restype = ctypes.c_int
         lib.oracle_to_gray8.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
         lib.oracle_to_gray8.restype = None
+        lib.oracle_morphology.argtypes = [_VIEW_P, _VIEW_P, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
+                                          ctypes.c_int, ctypes.c_int]
+        lib.oracle_morphology.restype = ctypes.c_int
         lib.oracle_sensitivity.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p, ctypes.c_int]
         lib.oracle_sensitivity.restype = ctypes.c_int
@@ -75,6 +78,9 @@ def ref_lib():
         lib = _load(HERE / "_ref" / "libiane_ref.so")
         lib.ref_convolve.argtypes = [_VIEW_P, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_int]
         lib.ref_convolve.restype = ctypes.c_int
+        lib.ref_morphology.argtypes = [_VIEW_P, _VIEW_P, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
+                                       ctypes.c_int, ctypes.c_int]
+        lib.ref_morphology.restype = ctypes.c_int
         lib.ref_rl.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
                                ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_float, ctypes.c_int,
                                ctypes.c_void_p, ctypes.c_int]
@@ -227,3 +233,30 @@ def wiener(observed: np.ndarray, psf: np.ndarray, noise: float, out_dtype=np.uin
     if np.dtype(out_dtype) == np.uint8:
         return to_gray8(r)
     return r.astype(out_dtype)
+
+
+MORPHOLOGY_OPS = {"erode": 0, "dilate": 1, "opening": 2, "closing": 3}
+
+
+def morphology(src: np.ndarray, out: np.ndarray, radius, op: str = "erode", border: str = "clamp",
+               footprint: np.ndarray | None = None, use_reference: bool = False) -> np.ndarray:
+    """Flat erosion / dilation, or opening / closing as the two passes through a packed
+    intermediate (morphology.hpp:118-125). ``radius`` is C-ordered like the arrays;
+    ``footprint`` (optional) is a boolean array of shape 2 * radius + 1 (C order)."""
+    if op in ("opening", "closing"):
+        first, second = ("erode", "dilate") if op == "opening" else ("dilate", "erode")
+        mid = np.zeros(src.shape, src.dtype)
+        morphology(src, mid, radius, first, border, footprint, use_reference)
+        return morphology(mid, out, radius, second, border, footprint, use_reference)
+    rank = src.ndim
+    r = (ctypes.c_int32 * 3)(*([int(radius[rank - 1 - i]) for i in range(rank)] + [0] * (3 - rank)))
+    mask = None
+    if footprint is not None:
+        mask = np.ascontiguousarray(footprint, dtype=np.uint8)
+    s, d = abi.numpy_view(src), abi.numpy_view(out)
+    fn = ref_lib().ref_morphology if use_reference else oracle_lib().oracle_morphology
+    status = fn(ctypes.byref(s), ctypes.byref(d), r, None if mask is None else mask.ctypes.data,
+                MORPHOLOGY_OPS[op], abi.BORDERS[border])
+    _check(status, "morphology")
+    return out
+

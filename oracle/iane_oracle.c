@@ -658,3 +658,69 @@ int oracle_sensitivity(const float* kernel, const int32_t* kernel_extent, int ra
 	free(ones);
 	return status;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* flat morphology                                                                        */
+
+/* erode / dilate (include/iane/algorithms/morphology/morphology.hpp:44-71): the footprint
+ * box of (2 r + 1) per axis scanned in raster order, offsets o = position - r, mask[q]
+ * selecting positions (NULL: all); erosion takes the minimum of src(p + o), dilation the
+ * maximum of src(p - o), with the rule `value < result` (`>`) from +inf / -inf (the type's
+ * max / lowest for integers), so NaN never replaces the running value and the first of
+ * equal values stays. Out-of-range zero-border samples are the value 0. Values are compared
+ * as doubles, which every supported element type converts to exactly. Single-threaded. */
+int oracle_morphology(const iane_gb_view* src, const iane_gb_view* dst, const int32_t* radius,
+	const uint8_t* mask, int dilate, int border)
+{
+	if (!check_view(src) || !check_view(dst) || src->rank != dst->rank || src->dtype != dst->dtype || !radius ||
+	    border < IANE_GB_BORDER_CLAMP || border > IANE_GB_BORDER_MIRROR) {
+		return ORACLE_EINVAL;
+	}
+	int64_t ext[3], r[3];
+	view_extents(src, ext);
+	for (int i = 0; i < 3; ++i) {
+		r[i] = i < src->rank ? radius[i] : 0;
+		if (r[i] < 0 || (i < src->rank && dst->extent[i] != src->extent[i])) {
+			return ORACLE_EINVAL;
+		}
+	}
+	double start;
+	switch (src->dtype) {
+	case IANE_GB_F32: case IANE_GB_F64: start = dilate ? -INFINITY : INFINITY; break;
+	case IANE_GB_U8: start = dilate ? 0.0 : 255.0; break;
+	case IANE_GB_I8: start = dilate ? -128.0 : 127.0; break;
+	case IANE_GB_U16: start = dilate ? 0.0 : 65535.0; break;
+	case IANE_GB_I16: start = dilate ? -32768.0 : 32767.0; break;
+	case IANE_GB_I32: start = dilate ? -2147483648.0 : 2147483647.0; break;
+	case IANE_GB_U32: start = dilate ? 0.0 : 4294967295.0; break;
+	default: return ORACLE_EINVAL;
+	}
+	for (int64_t z = 0; z < ext[2]; ++z)
+		for (int64_t y = 0; y < ext[1]; ++y)
+			for (int64_t x = 0; x < ext[0]; ++x) {
+				double m = start;
+				int64_t q = 0;
+				for (int64_t pz = 0; pz <= 2 * r[2]; ++pz)
+					for (int64_t py = 0; py <= 2 * r[1]; ++py)
+						for (int64_t px = 0; px <= 2 * r[0]; ++px, ++q) {
+							if (mask && !mask[q]) {
+								continue;
+							}
+							const int64_t ox = px - r[0], oy = py - r[1], oz = pz - r[2];
+							const int64_t sx = dilate ? x - ox : x + ox;
+							const int64_t sy = dilate ? y - oy : y + oy;
+							const int64_t sz = dilate ? z - oz : z + oz;
+							int64_t mx = 0, my = 0, mz = 0;
+							double v = 0.0;
+							if (map_coordinate(sx, ext[0], border, &mx) && map_coordinate(sy, ext[1], border, &my) &&
+							    map_coordinate(sz, ext[2], border, &mz)) {
+								v = load_double(view_at(src, mx, my, mz), src->dtype);
+							}
+							if (dilate ? v > m : v < m) {
+								m = v;
+							}
+						}
+				store_double((char*)view_at(dst, x, y, z), dst->dtype, m);
+			}
+	return ORACLE_OK;
+}

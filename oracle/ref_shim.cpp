@@ -13,6 +13,7 @@
 
 #include <iane/algorithms/convolution.hpp>
 #include <iane/algorithms/copy.hpp>
+#include <iane/algorithms/morphology/morphology.hpp>
 #include <iane/image/image.hpp>
 #include <iane/resource/host/resource_host.hpp>
 #include <iane/view/make_view.hpp>
@@ -217,9 +218,88 @@ int rl_typed(const float* aObserved, const int32_t* aExtent, const float* aPsf, 
 	return 0;
 }
 
+// A footprint predicate over a mask of (2 r + 1) per axis in raster order.
+template<int tDim>
+struct mask_predicate {
+	const std::uint8_t* mask;
+	extents_t<tDim> radius;
+
+	template<class TCoord>
+	bool operator()(const TCoord& aOffset) const
+	{
+		long long index = 0, stride = 1;
+		for (int i = 0; i < tDim; ++i) {
+			const int r = iane::math::detail::axis(radius, i);
+			index += (iane::math::detail::axis(aOffset, i) + r) * stride;
+			stride *= 2 * r + 1;
+		}
+		return mask[index] != 0;
+	}
+};
+
+template<class T, int tDim>
+int morphology_typed(const iane_gb_view& aSrc, const iane_gb_view& aDst, const int32_t* aRadius,
+	const std::uint8_t* aMask, int aDilate, int aBorder)
+{
+	const iane::const_host_image_view<T, tDim> src(static_cast<const T*>(aSrc.ptr),
+		to_extents<tDim>(aSrc.extent), to_strides<tDim>(aSrc.stride));
+	const iane::host_image_view<T, tDim> dst(static_cast<T*>(aDst.ptr),
+		to_extents<tDim>(aDst.extent), to_strides<tDim>(aDst.stride));
+	typename iane::math::dim_traits<tDim>::coord_t radius{};
+	for (int i = 0; i < tDim; ++i) iane::math::detail::axis(radius, i) = aRadius[i];
+	const iane::morphology_options options{
+		.border = aBorder == IANE_GB_BORDER_ZERO ? iane::border_mode::zero : iane::border_mode::clamp};
+	if (aMask) {
+		const auto footprint = iane::make_flat_footprint(radius, mask_predicate<tDim>{aMask, to_extents<tDim>(aRadius)});
+		if (aDilate) iane::dilate(src, dst, footprint, options).wait();
+		else iane::erode(src, dst, footprint, options).wait();
+	} else {
+		const auto footprint = iane::box_footprint(radius);
+		if (aDilate) iane::dilate(src, dst, footprint, options).wait();
+		else iane::erode(src, dst, footprint, options).wait();
+	}
+	return 0;
+}
+
+template<class T>
+int morphology_rank(const iane_gb_view& aSrc, const iane_gb_view& aDst, const int32_t* aRadius,
+	const std::uint8_t* aMask, int aDilate, int aBorder)
+{
+	switch (aSrc.rank) {
+	case 1: return morphology_typed<T, 1>(aSrc, aDst, aRadius, aMask, aDilate, aBorder);
+	case 2: return morphology_typed<T, 2>(aSrc, aDst, aRadius, aMask, aDilate, aBorder);
+	case 3: return morphology_typed<T, 3>(aSrc, aDst, aRadius, aMask, aDilate, aBorder);
+	default: return IANE_GB_UNSUPPORTED;
+	}
+}
+
 } // namespace
 
 extern "C" {
+
+// iane::erode / iane::dilate (include/iane/algorithms/morphology/morphology.hpp:172-206) on
+// host views, box footprint (mask NULL) or a mask predicate.
+int ref_morphology(const iane_gb_view* aSrc, const iane_gb_view* aDst, const int32_t* aRadius,
+	const std::uint8_t* aMask, int aDilate, int aBorder)
+{
+	if (!aSrc || !aDst || !aRadius || aSrc->rank != aDst->rank || aSrc->dtype != aDst->dtype ||
+	    (aBorder != IANE_GB_BORDER_ZERO && aBorder != IANE_GB_BORDER_CLAMP)) {
+		return IANE_GB_INVALID_ARGUMENT;
+	}
+	try {
+		switch (aSrc->dtype) {
+		case IANE_GB_U8: return morphology_rank<std::uint8_t>(*aSrc, *aDst, aRadius, aMask, aDilate, aBorder);
+		case IANE_GB_I16: return morphology_rank<std::int16_t>(*aSrc, *aDst, aRadius, aMask, aDilate, aBorder);
+		case IANE_GB_I32: return morphology_rank<std::int32_t>(*aSrc, *aDst, aRadius, aMask, aDilate, aBorder);
+		case IANE_GB_U32: return morphology_rank<std::uint32_t>(*aSrc, *aDst, aRadius, aMask, aDilate, aBorder);
+		case IANE_GB_F32: return morphology_rank<float>(*aSrc, *aDst, aRadius, aMask, aDilate, aBorder);
+		case IANE_GB_F64: return morphology_rank<double>(*aSrc, *aDst, aRadius, aMask, aDilate, aBorder);
+		default: return IANE_GB_UNSUPPORTED;
+		}
+	} catch (const std::exception&) {
+		return IANE_GB_INVALID_ARGUMENT;
+	}
+}
 
 int ref_convolve(const iane_gb_view* aSrc, const iane_gb_view* aKernel, const iane_gb_view* aDst,
 	int aBorder, int aThreads)

@@ -139,6 +139,36 @@ def main() -> int:
     oracle.convolve_rgb8(rgb, k, out, "clamp", use_reference=True)
     g["rgb8_bench_clamp__src"], g["rgb8_bench_clamp__kernel"], g["rgb8_bench_clamp__out"] = rgb, k, out
 
+    # Flat morphology through the reference's own erode / dilate (box footprints and mask
+    # predicates), own seed: float data with NaNs and signed zeros exercise the update rule.
+    rng3 = np.random.default_rng(20261205)
+
+    def morph(name, src, radius, op, border, mask=None):
+        out = np.zeros_like(src)
+        oracle.morphology(src, out, radius, op, border, mask, use_reference=True)
+        g[f"morph_{name}__src"], g[f"morph_{name}__out"] = src, out
+        g[f"morph_{name}__radius"] = np.array(radius, np.int32)
+        g[f"morph_{name}__op"], g[f"morph_{name}__border"] = np.array(op), np.array(border)
+        g[f"morph_{name}__mask"] = np.zeros(0, np.uint8) if mask is None else mask.astype(np.uint8)
+
+    morph("u8_2d_box_erode_clamp", rng3.integers(0, 256, (23, 31), dtype=np.uint8), (1, 2), "erode", "clamp")
+    morph("u8_2d_box_dilate_zero", rng3.integers(0, 256, (23, 31), dtype=np.uint8), (2, 1), "dilate", "zero")
+    fl = rng3.standard_normal((5, 9, 13)).astype(np.float32)
+    fl[fl > 1.5] = np.nan
+    fl[np.abs(fl) < 0.2] = 0.0
+    fl[(np.abs(fl) < 0.4) & (fl < 0)] = -0.0
+    morph("f32_3d_box_erode_zero", fl, (1, 1, 2), "erode", "zero")
+    morph("f32_3d_box_dilate_clamp", fl, (1, 2, 1), "dilate", "clamp")
+    cross = np.zeros((5, 3), bool)
+    cross[2, :] = True
+    cross[:, 1] = True
+    morph("i16_2d_mask_dilate_clamp", rng3.integers(-30000, 30000, (17, 19), dtype=np.int16), (2, 1), "dilate",
+          "clamp", cross)
+    ring = np.ones((3, 3, 3), bool)
+    ring[1, 1, 1] = False
+    morph("f64_3d_mask_erode_zero", rng3.standard_normal((6, 7, 8)), (1, 1, 1), "erode", "zero", ring)
+    morph("u32_1d_box_dilate_zero", rng3.integers(0, 2 ** 32, 40, dtype=np.uint32), (3,), "dilate", "zero")
+
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
     return 0

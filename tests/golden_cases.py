@@ -18,7 +18,7 @@ def data():
 
 def conv_cases():
     d = data()
-    names = sorted({k.split("__")[0] for k in d if k.endswith("__border")})
+    names = sorted({k.split("__")[0] for k in d if k.endswith("__border") and not k.startswith("morph_")})
     return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"], str(d[f"{n}__border"])) for n in names]
 
 
@@ -28,6 +28,18 @@ def rgb8_cases():
     d = data()
     names = sorted({k.split("__")[0] for k in d if k.startswith("rgb8_") and k.endswith("__src")})
     return [(n, d[f"{n}__src"], d[f"{n}__kernel"], d[f"{n}__out"], n.rsplit("_", 1)[1]) for n in names]
+
+
+def morph_cases():
+    """Erosion / dilation outputs of the reference: (name, src, radius, op, border, mask or None, out)."""
+    d = data()
+    names = sorted({k.split("__")[0] for k in d if k.startswith("morph_") and k.endswith("__src")})
+    out = []
+    for n in names:
+        mask = d[f"{n}__mask"]
+        out.append((n, d[f"{n}__src"], tuple(int(v) for v in d[f"{n}__radius"]), str(d[f"{n}__op"]),
+                    str(d[f"{n}__border"]), mask.astype(bool) if mask.size else None, d[f"{n}__out"]))
+    return out
 
 
 def mirror_cases():

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
-from golden_cases import bench_pattern, conv_cases, mirror_cases, rgb8_cases, rl_cases
+from golden_cases import bench_pattern, conv_cases, mirror_cases, morph_cases, rgb8_cases, rl_cases
 
 
 def test_known_answer_1d_flip_zero_border():
@@ -228,3 +228,57 @@ def test_wiener_oracle_known_answers():
 def test_to_gray8_rule():
     v = np.array([-1.0, 0.0, 0.49, 0.5, 1.5, 2.4999, 254.5, 255.0, 300.0, np.nan], np.float32)
     assert oracle.to_gray8(v).tolist() == [0, 0, 0, 1, 2, 2, 255, 255, 255, 0]
+
+
+# --- flat morphology --------------------------------------------------------------------------
+
+def test_morphology_known_answers():
+    # test/unit/algorithms/color_morphology_cases.hpp:87-117: values {99, 3, 1, 5, 2, 99},
+    # crop [1, 5); a 1-radius box with clamp, and the offset-+1-only footprint with zero
+    src = np.array([99, 3, 1, 5, 2, 99], np.int32)[1:5]
+    out = np.zeros(4, np.int32)
+    assert oracle.morphology(src, out, (1,), "erode").tolist() == [1, 1, 1, 2]
+    assert oracle.morphology(src, out, (1,), "dilate").tolist() == [3, 5, 5, 5]
+    forward = np.array([False, False, True])
+    assert oracle.morphology(src, out, (1,), "erode", "zero", forward).tolist() == [1, 5, 2, 0]
+    assert oracle.morphology(src, out, (1,), "dilate", "zero", forward).tolist() == [0, 3, 1, 5]
+
+
+def test_morphology_compound_known_answer():
+    # color_morphology_cases.hpp:119-166 in 3-D: a two-plane slab plus an impulse; opening
+    # removes the impulse and keeps the slab, closing the complement does the same
+    for close in (False, True):
+        img = np.zeros((3, 3, 4), np.int32)
+        img[:, :, :2] = 1
+        img[1, 1, 3] = 1
+        if close:
+            img = 1 - img
+        out = np.zeros_like(img)
+        oracle.morphology(img, out, (1, 1, 1), "closing" if close else "opening")
+        want = np.zeros_like(img)
+        want[:, :, :2] = 1
+        assert np.array_equal(out, 1 - want if close else want)
+
+
+@pytest.mark.parametrize("case", morph_cases(), ids=lambda c: c[0])
+def test_oracle_morphology_matches_golden(case):
+    name, src, radius, op, border, mask, expected = case
+    out = np.zeros_like(src)
+    oracle.morphology(src, out, radius, op, border, mask)
+    assert out.tobytes() == expected.tobytes(), name  # bitwise: NaN and signed zeros included
+
+
+@reference
+@pytest.mark.parametrize("dtype", [np.uint8, np.int16, np.float32])
+@pytest.mark.parametrize("border", ["clamp", "zero"])
+def test_oracle_morphology_matches_live_reference(dtype, border):
+    rng = np.random.default_rng(31)
+    src = (rng.standard_normal((4, 9, 11)) * 50).astype(dtype) if dtype == np.float32 else \
+        rng.integers(np.iinfo(dtype).min, np.iinfo(dtype).max, (4, 9, 11), dtype=dtype)
+    mask = rng.random((3, 5, 3)) < 0.5
+    for op in ("erode", "dilate"):
+        for m in (None, mask):
+            a, b = np.zeros_like(src), np.zeros_like(src)
+            oracle.morphology(src, a, (1, 2, 1), op, border, m)
+            oracle.morphology(src, b, (1, 2, 1), op, border, m, use_reference=True)
+            assert a.tobytes() == b.tobytes()
