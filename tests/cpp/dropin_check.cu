@@ -7,6 +7,7 @@
 #include <iane/resource/cuda/resource_cuda.hpp>
 #include <iane/resource/host/resource_host.hpp>
 #include <iane/gb/convolution.hpp>
+#include <iane/gb/morphology.hpp>
 
 #include <cmath>
 #include <cstdio>
@@ -59,6 +60,14 @@ static_assert(std::is_same_v<decltype(iane::convolve(std::declval<iane::const_de
 	std::declval<dev_k2>(), std::declval<iane::device_image_view<pixel3, 2>>())), iane::gb::execution>);
 static_assert(std::is_same_v<decltype(iane::convolve(std::declval<iane::texture_image_view<std::uint8_t, 2>>(),
 	std::declval<dev_k2>(), std::declval<dev_dst8>())), iane::gb::execution>);
+// ... and erosion / dilation of CUDA memory views, box or predicate footprints ...
+struct cross_predicate {
+	IANE_DECL_HYBRID bool operator()(const iane::math::vec2i& o) const { return o[0] == 0 || o[1] == 0; }
+};
+static_assert(std::is_same_v<decltype(iane::erode(std::declval<dev_src8>(), std::declval<dev_dst8>(),
+	iane::box_footprint(iane::math::vec2i{1, 2}))), iane::gb::execution>);
+static_assert(std::is_same_v<decltype(iane::dilate(std::declval<dev_src8>(), std::declval<dev_dst8>(),
+	iane::make_flat_footprint(iane::math::vec2i{1, 1}, cross_predicate{}))), iane::gb::execution>);
 // ... host views keep the reference's template.
 static_assert(!std::is_same_v<decltype(iane::convolve(std::declval<host_src>(), std::declval<host_src>(),
 	std::declval<host_dst>())), iane::gb::execution>);
@@ -155,6 +164,37 @@ int main()
 			}
 		}
 		std::printf("ok   texture convolution matches the reference\n");
+	}
+	{
+		// erosion with a predicate footprint and a prepared opening against the reference's CPU
+		iane::host_image<float, 3> ref_e(20, 18, 9), ref_o(20, 18, 9), mid(20, 18, 9);
+		struct odd_sum {
+			IANE_DECL_HYBRID bool operator()(const iane::math::vec3i& o) const { return ((o[0] + o[1] + o[2]) & 1) == 0; }
+		};
+		const auto fp = iane::make_flat_footprint(iane::math::vec3i{1, 2, 1}, odd_sum{});
+		iane::erode(h_src.const_view(), ref_e.view(), fp, {.border = iane::border_mode::zero});
+		iane::erode(h_src.const_view(), mid.view(), iane::box_footprint(iane::math::vec3i{1, 1, 1}));
+		iane::dilate(mid.const_view(), ref_o.view(), iane::box_footprint(iane::math::vec3i{1, 1, 1}));
+		iane::erode(d_src.const_view(), d_out.view(), fp, {.border = iane::border_mode::zero}).wait();
+		iane::copy(d_out.const_view(), h_out.view()).wait();
+		for (int i = 0; i < 20 * 18 * 9; ++i) {
+			if (h_out.pointer()[i] != ref_e.pointer()[i]) {
+				std::printf("FAIL erosion differs at %d\n", i);
+				return 1;
+			}
+		}
+		auto mexec = iane::make_execution_context(iane::cuda_policy{});
+		auto plan = mexec.prepare(iane::gb::opening(iane::box_footprint(iane::math::vec3i{1, 1, 1})), d_src.const_view(),
+			d_out.view());
+		mexec.run(plan, d_src.const_view(), d_out.view()).wait();
+		iane::copy(d_out.const_view(), h_out.view()).wait();
+		for (int i = 0; i < 20 * 18 * 9; ++i) {
+			if (h_out.pointer()[i] != ref_o.pointer()[i]) {
+				std::printf("FAIL opening differs at %d\n", i);
+				return 1;
+			}
+		}
+		std::printf("ok   morphology matches the reference\n");
 	}
 	auto exec = iane::make_execution_context(iane::cuda_policy{});
 	auto op = exec.prepare(iane::gb::richardson_lucy{d_k.const_view(), 5, 1e-6f, iane::gb::rl_start::mean},
