@@ -10,8 +10,9 @@
 // neighbourhood stays at the start value, and among equal values (-0 and +0) the first in
 // scan order wins (morphology.hpp:44-71).
 //
-// Box footprints run separably -- one kernel scans x then y in shared memory per plane, a
-// second scans z -- in the same order per axis as the reference's raster scan (reversed for
+// Box footprints run separably -- x then y in shared memory per plane, then z over a ring of
+// plane results in the same kernel (a second kernel for very deep z windows) -- in the same
+// order per axis as the reference's raster scan (reversed for
 // dilation, whose samples run p + r down to p - r). The first extreme of the raster scan is
 // the first extreme along z of the first along y of the first along x, so the separable
 // result is bit-identical, signed zeros included. Masked footprints (any subset of the box)
@@ -43,6 +44,16 @@ template<bool DILATE, class T> __device__ __forceinline__ void take(T v, T& r)
 	if (DILATE ? v > r : v < r) r = v;
 }
 
+// The reference's scan of 2 r + 1 taps from p with stride `step` (negative for dilation).
+template<bool DILATE, class T>
+__device__ __forceinline__ T scan(const T* p, int taps, int step)
+{
+	T m = start_value<T>(DILATE);
+#pragma unroll 4
+	for (int o = 0; o < taps; ++o, p += step) take<DILATE>(*p, m);
+	return m;
+}
+
 template<class T> __device__ __forceinline__ T sample(const DevView& v, int x, int y, int z, int border)
 {
 	int xi = 0, yi = 0, zi = 0;
@@ -50,6 +61,35 @@ template<class T> __device__ __forceinline__ T sample(const DevView& v, int x, i
 		return *element_ptr<T>(v, xi, yi, zi);
 	}
 	return T(0);
+}
+
+// Stage the (32 + 2 rx) x (32 + 2 ry) tile of plane zm (zok false: the zero plane) whose
+// corner is (x0 - rx, y0 - ry): one row per warp step, the row's y mapped once, interior rows
+// without per-element border mapping. 256 threads as 8 rows of 32.
+template<class T>
+__device__ __forceinline__ void load_tile(const DevView& src, T* tile, int x0, int y0, int rx, int ry, int zm, bool zok,
+	int border)
+{
+	const int tw = kTX + 2 * rx, th = kTY + 2 * ry;
+	const int gx0 = x0 - rx;
+	const bool x_inside = gx0 >= 0 && gx0 + tw <= src.ext[0];
+	for (int r = threadIdx.y; r < th; r += 8) {
+		int yi = 0;
+		const bool yok = zok && map_coord(y0 - ry + r, src.ext[1], border, yi);
+		const char* row = src.ptr + yi * src.stride[1] + zm * src.stride[2];
+		T* out = tile + r * tw;
+		if (!yok) {
+			for (int c = threadIdx.x; c < tw; c += 32) out[c] = T(0);
+		} else if (x_inside) {
+			for (int c = threadIdx.x; c < tw; c += 32) out[c] = *reinterpret_cast<const T*>(row + (gx0 + c) * src.stride[0]);
+		} else {
+			for (int c = threadIdx.x; c < tw; c += 32) {
+				int xi = 0;
+				out[c] = map_coord(gx0 + c, src.ext[0], border, xi) ? *reinterpret_cast<const T*>(row + xi * src.stride[0])
+					: T(0);
+			}
+		}
+	}
 }
 
 // Box footprint, x then y, for one 32x32 output tile of plane blockIdx.z. Shared memory: the
@@ -61,19 +101,12 @@ __global__ void __launch_bounds__(256) morph_box_xy_kernel(DevView src, DevView 
 	const int tw = kTX + 2 * rx, th = kTY + 2 * ry;
 	T* tile = reinterpret_cast<T*>(smem_raw);
 	T* xbuf = tile + tw * th;
-	const int tid = threadIdx.y * 32 + threadIdx.x;
 	const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z = blockIdx.z;
-	for (int i = tid; i < tw * th; i += 256) {
-		const int r = i / tw, c = i - r * tw;
-		tile[i] = sample<T>(src, x0 - rx + c, y0 - ry + r, z, border);
-	}
+	load_tile<T>(src, tile, x0, y0, rx, ry, z, true, border);
 	__syncthreads();
-	for (int i = tid; i < kTX * th; i += 256) {
-		const int r = i / kTX, c = i - r * kTX;
-		T m = start_value<T>(DILATE);
-		const T* row = tile + r * tw + c;
-		for (int o = 0; o <= 2 * rx; ++o) take<DILATE>(row[DILATE ? 2 * rx - o : o], m);
-		xbuf[i] = m;
+	for (int r = threadIdx.y; r < th; r += 8) {
+		xbuf[r * kTX + threadIdx.x] =
+			scan<DILATE>(tile + r * tw + threadIdx.x + (DILATE ? 2 * rx : 0), 2 * rx + 1, DILATE ? -1 : 1);
 	}
 	__syncthreads();
 	const int x = x0 + threadIdx.x;
@@ -82,9 +115,69 @@ __global__ void __launch_bounds__(256) morph_box_xy_kernel(DevView src, DevView 
 		const int r = threadIdx.y + 8 * k;
 		const int y = y0 + r;
 		if (y >= dst.ext[1]) break;
-		T m = start_value<T>(DILATE);
-		for (int o = 0; o <= 2 * ry; ++o) take<DILATE>(xbuf[(r + (DILATE ? 2 * ry - o : o)) * kTX + threadIdx.x], m);
-		*const_cast<T*>(element_ptr<T>(dst, x, y, z)) = m;
+		*const_cast<T*>(element_ptr<T>(dst, x, y, z)) = scan<DILATE>(
+			xbuf + (r + (DILATE ? 2 * ry : 0)) * kTX + threadIdx.x, 2 * ry + 1, DILATE ? -kTX : kTX);
+	}
+}
+
+// Box footprint in 3-D, fused: the block owns a 32x32 column of planes [z0, z0 + zc). Each
+// input plane of [z0 - rz, z0 + zc + rz) is staged, reduced along x then y into a ring of
+// 2 rz + 1 xy-results in shared memory, and every output plane whose z window is complete is
+// reduced over the ring in scan order (increasing z for erosion, decreasing for dilation):
+// one read of each input plane per chunk (plus 2 rz halo planes) and one write per output.
+template<class T, bool DILATE>
+__global__ void __launch_bounds__(256) morph_box_3d_kernel(DevView src, DevView dst, int rx, int ry, int rz, int zc,
+	int border)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const int tw = kTX + 2 * rx, th = kTY + 2 * ry;
+	const int depth = 2 * rz + 1;
+	T* ring = reinterpret_cast<T*>(smem_raw);      // depth x 32 x 32
+	T* tile = ring + depth * kTX * kTY;            // tw x th
+	T* xbuf = tile + tw * th;                      // 32 x th
+	const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+	const int z0 = blockIdx.z * zc;
+	const int z1 = min(dst.ext[2], z0 + zc);
+	const int nz = src.ext[2];
+	int slot_new = 0; // ring slot of plane zi: (zi - (z0 - rz)) mod depth
+	for (int zi = z0 - rz; zi < z1 + rz; ++zi, slot_new = slot_new + 1 == depth ? 0 : slot_new + 1) {
+		int zm = 0;
+		const bool zok = map_coord(zi, nz, border, zm);
+		load_tile<T>(src, tile, x0, y0, rx, ry, zm, zok, border);
+		__syncthreads();
+		for (int r = threadIdx.y; r < th; r += 8) {
+			xbuf[r * kTX + threadIdx.x] =
+				scan<DILATE>(tile + r * tw + threadIdx.x + (DILATE ? 2 * rx : 0), 2 * rx + 1, DILATE ? -1 : 1);
+		}
+		__syncthreads();
+		T* slot = ring + slot_new * (kTX * kTY);
+		for (int k = 0; k < kTY / 8; ++k) {
+			const int r = threadIdx.y + 8 * k;
+			slot[r * kTX + threadIdx.x] = scan<DILATE>(
+				xbuf + (r + (DILATE ? 2 * ry : 0)) * kTX + threadIdx.x, 2 * ry + 1, DILATE ? -kTX : kTX);
+		}
+		__syncthreads();
+		const int zo = zi - rz; // the output plane whose window ends at zi
+		if (zo >= z0) {
+			const int x = x0 + threadIdx.x;
+			if (x < dst.ext[0]) {
+				for (int k = 0; k < kTY / 8; ++k) {
+					const int r = threadIdx.y + 8 * k;
+					const int y = y0 + r;
+					if (y >= dst.ext[1]) break;
+					// the window zo - rz .. zo + rz = the ring's planes, the oldest in slot_new + 1
+					T m = start_value<T>(DILATE);
+					int sl = DILATE ? slot_new : (slot_new + 1 == depth ? 0 : slot_new + 1);
+					for (int o = 0; o <= 2 * rz; ++o) {
+						take<DILATE>(ring[sl * (kTX * kTY) + r * kTX + threadIdx.x], m);
+						sl = DILATE ? (sl == 0 ? depth - 1 : sl - 1) : (sl + 1 == depth ? 0 : sl + 1);
+					}
+					*const_cast<T*>(element_ptr<T>(dst, x, y, zo)) = m;
+				}
+			}
+		}
+		// the next plane's y pass overwrites the oldest ring slot only after the barriers of
+		// its tile and x passes, which every thread reaches after this reduction
 	}
 }
 
@@ -136,6 +229,11 @@ size_t box_xy_smem(int rx, int ry, int esize)
 	return static_cast<size_t>((kTX + 2 * rx) * (kTY + 2 * ry) + kTX * (kTY + 2 * ry)) * esize;
 }
 
+size_t box_3d_smem(int rx, int ry, int rz, int esize)
+{
+	return box_xy_smem(rx, ry, esize) + static_cast<size_t>(2 * rz + 1) * kTX * kTY * esize;
+}
+
 template<class T, bool DILATE>
 int launch_op(const DevView& s, const DevView& d, const int* r, const uint8_t* mask, int border, void* temp,
 	cudaStream_t st)
@@ -161,7 +259,21 @@ int launch_op(const DevView& s, const DevView& d, const int* r, const uint8_t* m
 		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
 		return IANE_GB_OK;
 	}
-	// 3-D box: xy into a packed temporary, then z into the destination
+	const size_t smem3 = box_3d_smem(r[0], r[1], r[2], sizeof(T));
+	if (smem3 <= 100 * 1024) {
+		// fused 3-D box: chunks of zc output planes per block, enough blocks to fill the GPU
+		const long long tiles = static_cast<long long>(gt.x) * gt.y;
+		int zc = 32;
+		while (zc > 4 && tiles * ((d.ext[2] + zc - 1) / zc) < 8LL * device_sm_count()) zc /= 2;
+		auto k3 = morph_box_3d_kernel<T, DILATE>;
+		IANE_GB_CUDA(cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem3)),
+			"morphology: shared memory");
+		const dim3 g3(gt.x, gt.y, (d.ext[2] + zc - 1) / zc);
+		k3<<<g3, dim3(32, 8), smem3, st>>>(s, d, r[0], r[1], r[2], zc, border);
+		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
+		return IANE_GB_OK;
+	}
+	// 3-D box with a deep z window: xy into a packed temporary, then z into the destination
 	DevView t{};
 	t.ptr = static_cast<char*>(temp);
 	t.dtype = d.dtype;
@@ -270,7 +382,8 @@ int iane_gb_morphology(const iane_gb_view* src, const iane_gb_view* dst, const i
 	if (status) return status;
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	void* temp = nullptr;
-	const bool needs_temp = !footprint && r[2] > 0 && box_xy_smem(r[0], r[1], dtype_size(d.dtype)) <= 200 * 1024;
+	const bool needs_temp = !footprint && r[2] > 0 && box_xy_smem(r[0], r[1], dtype_size(d.dtype)) <= 200 * 1024 &&
+		box_3d_smem(r[0], r[1], r[2], dtype_size(d.dtype)) > 100 * 1024;
 	if (needs_temp) {
 		IANE_GB_CUDA(cudaMallocAsync(&temp, packed_bytes(d), st), "morphology: temporary");
 	}
