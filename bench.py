@@ -185,7 +185,7 @@ def measure_hbm_legs(dev, stream, reps=20, cpu=True):
     512^3 f32 volume (7-tap Gaussians, mirror border; 1 GiB in + out, larger than L2), the
     2-D 512x512 7x7 Gaussian mirror configuration, direct and separable (with the host
     baseline: the oracle port of the reference's convolve on all host threads and on one),
-    and the same 2-D filter at 8192x8192 where bandwidth can be judged. Device time per
+    and the same 2-D filter at 8192x8192 where bandwidth dominates. Device time per
     launch (CUDA events), algorithmic bytes = 8 per voxel (one read, one write)."""
     import numpy as np
     import torch
