@@ -86,7 +86,7 @@ __global__ void batch_init_kernel(const InitDesc* d, const float* starts, float 
 	}
 }
 
-int occupancy_grid(int wx, size_t smem, size_t items);
+int occupancy_grid(int wx, bool wide, size_t smem, size_t items);
 
 bool work_layout(const DevView& v, long long pitch)
 {
@@ -121,7 +121,7 @@ std::string cache_path()
 std::string tune_key(int nx, int ny, int kx, int ky)
 {
 	std::ostringstream k;
-	k << "rl2d f32 " << nx << "x" << ny << " psf " << kx << "x" << ky << " sms " << device_sm_count();
+	k << "rl2d-classes f32 " << nx << "x" << ny << " psf " << kx << "x" << ky << " sms " << device_sm_count();
 	return k.str();
 }
 
@@ -228,11 +228,11 @@ int batch_autotune(const std::vector<int>& nx, const std::vector<int>& ny, const
 				return release(cuda_fail(cudaGetLastError(), "autotune: upload"));
 			}
 			const size_t smem = batch_tile_smem(w, kx[i], ky[i]);
-			const int grid = occupancy_grid(w, smem, items.size());
+			const int grid = occupancy_grid(w, batch_wide(kx[i]), smem, items.size());
 			for (int rep = 0; rep < 4; ++rep) {
 				if (rep == 1) cudaEventRecord(t0, stream);
 				cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream);
-				st = launch_batch_pass(w, false, d_images, d_items, static_cast<int>(items.size()), counter, 0, grid, smem,
+				st = launch_batch_pass(w, batch_wide(kx[i]), false, d_images, d_items, static_cast<int>(items.size()), counter, 0, grid, smem,
 					stream);
 				if (st) return release(st);
 			}
@@ -258,15 +258,17 @@ struct iane_gb_rl_batch {
 	std::vector<long long> pitch;
 	std::vector<size_t> off;               // per image: ratio at off, work at off + image bytes
 	std::vector<size_t> img_bytes;
-	std::vector<iane_gb::BatchItem> items[2];  // [0]: 32x32 tiles, [1]: 64x64 tiles
-	iane_gb::BatchItem* d_items[2] = {nullptr, nullptr};
-	size_t smem[2] = {0, 0};
-	int grid[2] = {0, 0};
+	// per group (batch_group: 32x32 / 64x64 tiles x narrow / wide PSFs)
+	std::vector<iane_gb::BatchItem> items[iane_gb::kBatchGroups];
+	iane_gb::BatchItem* d_items[iane_gb::kBatchGroups] = {};
+	size_t smem[iane_gb::kBatchGroups] = {};
+	int grid[iane_gb::kBatchGroups] = {};
 	iane_gb::BatchImage* d_images = nullptr;
 	iane_gb::InitDesc* d_init = nullptr;
 	size_t parts_off = 0, counter_off = 0, scratch_bytes = 0;
-	cudaStream_t side[2] = {nullptr, nullptr};
-	cudaEvent_t fork = nullptr, join = nullptr;
+	cudaStream_t side[iane_gb::kBatchGroups] = {};  // side[0] carries the capture
+	cudaEvent_t fork = nullptr;
+	cudaEvent_t join[iane_gb::kBatchGroups] = {};
 	cudaGraphExec_t exec = nullptr;
 	std::string key;
 };
@@ -328,7 +330,7 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 	double* parts = reinterpret_cast<double*>(base + b->parts_off);
 	float* starts = reinterpret_cast<float*>(parts);
 	unsigned int* counters = reinterpret_cast<unsigned int*>(base + b->counter_off);
-	cudaStream_t s0 = b->side[0], s1 = b->side[1];
+	cudaStream_t s0 = b->side[0];
 	cudaGraph_t graph = nullptr;
 	IANE_GB_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal), "batch: begin capture");
 	auto abort_capture = [&](int code) {
@@ -337,7 +339,8 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 		if (g) cudaGraphDestroy(g);
 		return code;
 	};
-	if (cudaMemsetAsync(counters, 0, static_cast<size_t>(4 * iterations + 4) * sizeof(unsigned int), s0) != cudaSuccess) {
+	if (cudaMemsetAsync(counters, 0, static_cast<size_t>(2 * kBatchGroups * (iterations + 1)) * sizeof(unsigned int),
+	        s0) != cudaSuccess) {
 		return abort_capture(cuda_fail(cudaGetLastError(), "batch: clear counters"));
 	}
 	if (init == IANE_GB_RL_INIT_MEAN) {
@@ -346,19 +349,29 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 	batch_init_kernel<<<dim3(n, 16), 256, 0, s0>>>(b->d_init, starts, eps, init);
 	for (int t = 0; t < iterations; ++t) {
 		for (int pass = 0; pass < 2; ++pass) {
-			unsigned int* c = counters + 4 * t + 2 * pass;
-			if (cudaEventRecord(b->fork, s0) != cudaSuccess || cudaStreamWaitEvent(s1, b->fork, 0) != cudaSuccess) {
+			unsigned int* c = counters + 2 * kBatchGroups * t + kBatchGroups * pass;
+			if (cudaEventRecord(b->fork, s0) != cudaSuccess) {
 				return abort_capture(cuda_fail(cudaGetLastError(), "batch: fork"));
 			}
-			int st = launch_batch_pass(2, pass == 1, b->d_images, b->d_items[1], static_cast<int>(b->items[1].size()),
-				c + 1, t == iterations - 1, b->grid[1], b->smem[1], s0);
-			if (!st) {
-				st = launch_batch_pass(1, pass == 1, b->d_images, b->d_items[0], static_cast<int>(b->items[0].size()),
-					c, t == iterations - 1, b->grid[0], b->smem[0], s1);
+			for (int g = 1; g < kBatchGroups; ++g) {
+				if (!b->items[g].empty() && cudaStreamWaitEvent(b->side[g], b->fork, 0) != cudaSuccess) {
+					return abort_capture(cuda_fail(cudaGetLastError(), "batch: fork"));
+				}
 			}
-			if (st) return abort_capture(st);
-			if (cudaEventRecord(b->join, s1) != cudaSuccess || cudaStreamWaitEvent(s0, b->join, 0) != cudaSuccess) {
-				return abort_capture(cuda_fail(cudaGetLastError(), "batch: join"));
+			// the larger groups first on the capture stream; every group on its own branch
+			for (int g = 0; g < kBatchGroups; ++g) {
+				if (b->items[g].empty()) continue;
+				const int st = launch_batch_pass(1 + (g & 1), (g & 2) != 0, pass == 1, b->d_images, b->d_items[g],
+					static_cast<int>(b->items[g].size()), c + g, t == iterations - 1, b->grid[g], b->smem[g],
+					g == 0 ? s0 : b->side[g]);
+				if (st) return abort_capture(st);
+			}
+			for (int g = 1; g < kBatchGroups; ++g) {
+				if (b->items[g].empty()) continue;
+				if (cudaEventRecord(b->join[g], b->side[g]) != cudaSuccess ||
+				    cudaStreamWaitEvent(s0, b->join[g], 0) != cudaSuccess) {
+					return abort_capture(cuda_fail(cudaGetLastError(), "batch: join"));
+				}
 			}
 		}
 	}
@@ -376,24 +389,20 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 	return IANE_GB_OK;
 }
 
-int occupancy_grid(int wx, size_t smem, size_t items)
+int occupancy_grid(int wx, bool wide, size_t smem, size_t items)
 {
 	int per_sm = 1;
 	const size_t total = smem + 32;
-	if (wx == 1) {
-		cudaFuncSetAttribute(batch_kernel_handle(1), cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(total));
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_handle(1), 32, total);
-	} else {
-		cudaFuncSetAttribute(batch_kernel_handle(2), cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(total));
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_handle(2), 128, total);
-	}
+	const void* kernel = batch_kernel_handle(wx, wide);
+	cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(total));
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * wx * wx, total);
 	const long long g = static_cast<long long>(device_sm_count()) * std::max(1, per_sm);
 	return static_cast<int>(std::max<long long>(1, std::min<long long>(g, static_cast<long long>(items))));
 }
 
 void fill_items(iane_gb_rl_batch* b)
 {
-	for (int s = 0; s < 2; ++s) b->items[s].clear();
+	for (int g = 0; g < kBatchGroups; ++g) b->items[g].clear();
 	std::vector<int> order(b->count);
 	for (int i = 0; i < b->count; ++i) order[i] = i;
 	// group images by PSF width so that consecutive work items run the same kernel code
@@ -401,8 +410,9 @@ void fill_items(iane_gb_rl_batch* b)
 	for (int i : order) {
 		const int w = b->wx[i], t = 32 * w;
 		const int tiles = ((b->nx[i] + t - 1) / t) * ((b->ny[i] + t - 1) / t);
-		for (int k = 0; k < tiles; ++k) b->items[w - 1].push_back(BatchItem{i, k});
-		b->smem[w - 1] = std::max(b->smem[w - 1], batch_tile_smem(w, b->kx[i], b->ky[i]));
+		const int g = batch_group(w, b->kx[i]);
+		for (int k = 0; k < tiles; ++k) b->items[g].push_back(BatchItem{i, k});
+		b->smem[g] = std::max(b->smem[g], batch_tile_smem(w, b->kx[i], b->ky[i]));
 	}
 }
 
@@ -417,15 +427,15 @@ int iane_gb_rl_batch_destroy(iane_gb_rl_batch* b)
 {
 	if (!b) return IANE_GB_OK;
 	for (auto* p : b->plans) iane_gb_rl_destroy(p);
-	cudaFree(b->d_items[0]);
-	cudaFree(b->d_items[1]);
+	for (int g = 0; g < kBatchGroups; ++g) cudaFree(b->d_items[g]);
 	cudaFree(b->d_images);
 	cudaFree(b->d_init);
 	if (b->exec) cudaGraphExecDestroy(b->exec);
 	if (b->fork) cudaEventDestroy(b->fork);
-	if (b->join) cudaEventDestroy(b->join);
-	if (b->side[0]) cudaStreamDestroy(b->side[0]);
-	if (b->side[1]) cudaStreamDestroy(b->side[1]);
+	for (int g = 0; g < kBatchGroups; ++g) {
+		if (b->join[g]) cudaEventDestroy(b->join[g]);
+		if (b->side[g]) cudaStreamDestroy(b->side[g]);
+	}
 	delete b;
 	return IANE_GB_OK;
 }
@@ -481,25 +491,28 @@ int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t*
 	b->parts_off = off;
 	off += align_up(static_cast<size_t>(count) * sizeof(float));
 	b->counter_off = off;
-	off += align_up(static_cast<size_t>(4 * kMaxBatchIterations + 4) * sizeof(unsigned int));
+	off += align_up(static_cast<size_t>(2 * kBatchGroups * (kMaxBatchIterations + 1)) * sizeof(unsigned int));
 	b->scratch_bytes = off + kAlignB;
 	fill_items(b);
-	for (int s = 0; s < 2; ++s) {
-		if (b->items[s].empty()) continue;
-		b->grid[s] = occupancy_grid(s + 1, b->smem[s], b->items[s].size());
-		if (cudaMalloc(&b->d_items[s], b->items[s].size() * sizeof(BatchItem)) != cudaSuccess ||
-		    cudaMemcpy(b->d_items[s], b->items[s].data(), b->items[s].size() * sizeof(BatchItem),
+	for (int g = 0; g < kBatchGroups; ++g) {
+		if (b->items[g].empty()) continue;
+		b->grid[g] = occupancy_grid(1 + (g & 1), (g & 2) != 0, b->smem[g], b->items[g].size());
+		if (cudaMalloc(&b->d_items[g], b->items[g].size() * sizeof(BatchItem)) != cudaSuccess ||
+		    cudaMemcpy(b->d_items[g], b->items[g].data(), b->items[g].size() * sizeof(BatchItem),
 		        cudaMemcpyHostToDevice) != cudaSuccess) {
 			return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: upload work items"));
 		}
 	}
 	if (cudaMalloc(&b->d_images, count * sizeof(BatchImage)) != cudaSuccess ||
 	    cudaMalloc(&b->d_init, count * sizeof(InitDesc)) != cudaSuccess ||
-	    cudaStreamCreateWithFlags(&b->side[0], cudaStreamNonBlocking) != cudaSuccess ||
-	    cudaStreamCreateWithFlags(&b->side[1], cudaStreamNonBlocking) != cudaSuccess ||
-	    cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
-	    cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+	    cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
 		return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: allocate descriptors"));
+	}
+	for (int g = 0; g < kBatchGroups; ++g) {
+		if (cudaStreamCreateWithFlags(&b->side[g], cudaStreamNonBlocking) != cudaSuccess ||
+		    cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming) != cudaSuccess) {
+			return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: allocate streams"));
+		}
 	}
 	*out = b;
 	return IANE_GB_OK;

@@ -1,0 +1,8 @@
+// Batch-pass kernel: 32x32 tiles, pass A, narrow PSFs.
+#include "rl_batch_kernel.cuh"
+
+namespace iane_gb {
+
+IANE_GB_BATCH_LAUNCHER(1, false, false)
+
+}  // namespace iane_gb

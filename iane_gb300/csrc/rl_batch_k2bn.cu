@@ -1,0 +1,14 @@
+// Batch-pass kernel: 64x64 tiles, pass B, narrow PSFs.
+#include "rl_batch_kernel.cuh"
+
+namespace iane_gb {
+
+IANE_GB_BATCH_LAUNCHER(2, true, false)
+
+template<>
+const void* batch_kernel_handle_impl<2, false>()
+{
+	return reinterpret_cast<const void*>(batch_pass_kernel<2, true, false>);
+}
+
+}  // namespace iane_gb

@@ -9,26 +9,32 @@ namespace iane_gb {
 // Bytes after the largest tiles/taps of a launch: the two tile mbarriers and the work item.
 constexpr size_t kBatchTail = 32;
 
-template<int WX, bool PASS_B, class Epi>
+template<int WX, bool PASS_B, bool WIDE, class Epi>
 __device__ __forceinline__ void batch_run_item(const BatchImage& im, Epi& epi, int x0, int y0, uint32_t& phases,
 	uint64_t* bars)
 {
 	const CUtensorMap* map = PASS_B ? &im.map_ratio : &im.map_est;
 	const TileArgs& a = PASS_B ? im.pass_b : im.pass_a;
-	switch (im.kx) {
 #define IANE_GB_BATCH_KX(K) \
 	case K: conv_tile_body<K, WX, WX, kTileTma, Epi, true>(map, a, epi, x0, y0, 0, phases, bars); break;
-	IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
-	IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
-	IANE_GB_BATCH_KX(17) IANE_GB_BATCH_KX(19) IANE_GB_BATCH_KX(21) IANE_GB_BATCH_KX(23)
-	IANE_GB_BATCH_KX(25) IANE_GB_BATCH_KX(27) IANE_GB_BATCH_KX(29) IANE_GB_BATCH_KX(31)
-#undef IANE_GB_BATCH_KX
-	default: break;
+	if constexpr (WIDE) {
+		switch (im.kx) {
+		IANE_GB_BATCH_KX(17) IANE_GB_BATCH_KX(19) IANE_GB_BATCH_KX(21) IANE_GB_BATCH_KX(23)
+		IANE_GB_BATCH_KX(25) IANE_GB_BATCH_KX(27) IANE_GB_BATCH_KX(29) IANE_GB_BATCH_KX(31)
+		default: break;
+		}
+	} else {
+		switch (im.kx) {
+		IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
+		IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
+		default: break;
+		}
 	}
+#undef IANE_GB_BATCH_KX
 }
 
 // total = dynamic shared memory of the launch: the largest tiles/taps + kBatchTail.
-template<int WX, bool PASS_B>
+template<int WX, bool PASS_B, bool WIDE>
 __global__ void __launch_bounds__(32 * WX * WX) batch_pass_kernel(const BatchImage* __restrict__ images,
 	const BatchItem* __restrict__ items, int count, unsigned int* counter, int last, unsigned int total)
 {
@@ -58,19 +64,35 @@ __global__ void __launch_bounds__(32 * WX * WX) batch_pass_kernel(const BatchIma
 		if constexpr (PASS_B) {
 			EpiUpdate epi = im.epi_b;
 			epi.write_out = last && im.write_out_final;
-			batch_run_item<WX, true>(im, epi, x0, y0, phases, bars);
+			batch_run_item<WX, true, WIDE>(im, epi, x0, y0, phases, bars);
 		} else {
 			EpiRatio epi = im.epi_a;
-			batch_run_item<WX, false>(im, epi, x0, y0, phases, bars);
+			batch_run_item<WX, false, WIDE>(im, epi, x0, y0, phases, bars);
 		}
 	}
 }
 
-template<int WX, bool PASS_B>
+template<int WX, bool PASS_B, bool WIDE>
 int launch_batch_kernel(const BatchImage* images, const BatchItem* items, int count, unsigned int* counter, int last,
 	int grid, size_t total, cudaStream_t stream);
 
-template<int WX>
+template<int WX, bool WIDE>
 const void* batch_kernel_handle_impl();
+
+// One kernel variant per translation unit (rl_batch_k*.cu), so that they compile in parallel;
+// the pass-B variant also answers occupancy queries for its shape and class.
+#define IANE_GB_BATCH_LAUNCHER(WXV, PB, WD)                                                                  \
+	template<>                                                                                              \
+	int launch_batch_kernel<WXV, PB, WD>(const BatchImage* images, const BatchItem* items, int count,       \
+		unsigned int* counter, int last, int grid, size_t total, cudaStream_t stream)                       \
+	{                                                                                                       \
+		auto kernel = batch_pass_kernel<WXV, PB, WD>;                                                       \
+		IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,              \
+			static_cast<int>(total)), "batch pass: set shared memory size");                                \
+		kernel<<<grid, 32 * WXV * WXV, total, stream>>>(images, items, count, counter, last,               \
+			static_cast<unsigned int>(total));                                                              \
+		IANE_GB_CUDA(cudaGetLastError(), "batch pass: launch");                                             \
+		return IANE_GB_OK;                                                                                  \
+	}
 
 }  // namespace iane_gb
