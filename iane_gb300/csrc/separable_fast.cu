@@ -20,6 +20,8 @@
 #include "common.cuh"
 #include "kernels.h"
 
+#include <algorithm>
+
 namespace iane_gb {
 namespace {
 
@@ -69,13 +71,23 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	uint64_t* bars = reinterpret_cast<uint64_t*>(tpair + 2 * 16);
 
 	const int tid = threadIdx.x;
-	const int x0 = blockIdx.x * kFX, y0 = blockIdx.y * kFY;
+	const int x0 = blockIdx.x * kFX;
 	const int zs = Z ? blockIdx.z * a.zchunk : 0;
 	const int ze = Z ? min(zs + a.zchunk, a.nz) : 1;
-	const int nplanes = Z ? (ze - zs) + 2 * R : 1;
-	const bool interior = x0 - G::RA >= 0 && x0 + kFX + G::RA <= a.nx && y0 - R >= 0 && y0 + kFY + R <= a.ny;
+	// 3-D: the block's planes stream through the buffers. 2-D: its tiles do -- tile p is tile
+	// row blockIdx.y + p * gridDim.y, so consecutive tiles' loads overlap their filtering.
+	const int ytiles = (a.ny + kFY - 1) / kFY;
+	const int nplanes = Z ? (ze - zs) + 2 * R
+		: (ytiles - static_cast<int>(blockIdx.y) + static_cast<int>(gridDim.y) - 1) / static_cast<int>(gridDim.y);
+	auto y0_of = [&](int p) -> int {
+		return Z ? static_cast<int>(blockIdx.y) * kFY : (static_cast<int>(blockIdx.y) + p * static_cast<int>(gridDim.y)) * kFY;
+	};
 	const bool tma = a.use_tma;
-	const bool fixup = tma && !interior && a.border != IANE_GB_BORDER_ZERO;
+	auto fixup_of = [&](int p) -> bool {
+		const int y0 = y0_of(p);
+		const bool interior = x0 - G::RA >= 0 && x0 + kFX + G::RA <= a.nx && y0 - R >= 0 && y0 + kFY + R <= a.ny;
+		return tma && !interior && a.border != IANE_GB_BORDER_ZERO;
+	};
 
 	// Taps centred and zero-padded to 2R + 1; an axis beyond the rank is the single tap 1.
 	auto tap = [&](int axis, int i) -> float {
@@ -106,16 +118,16 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	};
 	auto issue = [&](int p) {
 		float* dst = A + (p % kNBuf) * G::A_FLOATS;
+		const int y0 = y0_of(p);
 		int zi = 0;
 		const bool present = plane_of(p, zi);
 		if (tma) {
 			// every plane gets one TMA (an out-of-volume plane reads as zeros), so the k-th
 			// completion of buffer b belongs to plane b + k * kNBuf
 			if (tid == 0) {
-				if (fixup) {
-					// order this buffer's earlier generic-proxy writes (the fix-up) before the TMA
-					asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-				}
+				// order this buffer's earlier generic-proxy use (a previous tile's fix-up) before
+				// the TMA's async-proxy write
+				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 				mbar_arrive_expect_tx(&bars[p % kNBuf], static_cast<uint32_t>(G::AW * G::AH * 4));
 				tma_load_3d(dst, &map, x0 - G::RA, y0 - R, present ? zi : (Z ? zs - R + p : 0), &bars[p % kNBuf]);
 			}
@@ -137,7 +149,7 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	// thread roles
 	const int xq = tid & 15, rg = tid >> 4;   // axis 0: 4 consecutive x of rows rg, rg + 16
 	const int xp = tid & 31, yq = tid >> 5;   // axes 1, 2: x pair 2xp, y rows 2yq, 2yq + 1
-	const int ox = x0 + 2 * xp, oy = y0 + 2 * yq;
+	const int ox = x0 + 2 * xp;
 
 	float2 win[2][K]; // axis-2 window: [row][plane slot]
 #pragma unroll
@@ -171,9 +183,10 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 				cp_async_wait<0>();
 			}
 		}
-		if (fixup) {
+		if (fixup_of(p)) {
 			// clamp / mirror: replace the zero-filled out-of-image halo cells by the cells the
 			// border rule maps them to (inside this tile, else read from the image)
+			const int y0 = y0_of(p);
 			float* tile = A + (p % kNBuf) * G::A_FLOATS;
 			int zi2 = 0;
 			plane_of(p, zi2);
@@ -242,10 +255,10 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 		}
 	};
 
-	auto store = [&](int zo, const float2& v0, const float2& v1) {
+	auto store = [&](int zo, int y0, const float2& v0, const float2& v1) {
 #pragma unroll
 		for (int j = 0; j < 2; ++j) {
-			const int y = oy + j;
+			const int y = y0 + 2 * yq + j;
 			const float2 v = j == 0 ? v0 : v1;
 			if (y < a.ny) {
 				char* row = a.dst + y * a.d_stride[1] + zo * a.d_stride[2];
@@ -260,9 +273,11 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 	};
 
 	if constexpr (!Z) {
-		float2 c0, c1;
-		filter_plane(0, c0, c1);
-		store(0, c0, c1);
+		for (int p = 0; p < nplanes; ++p) {
+			float2 c0, c1;
+			filter_plane(p, c0, c1);
+			store(0, y0_of(p), c0, c1);
+		}
 	} else {
 		for (int p = 0; p < nplanes; ++p) {
 			float2 n0, n1;
@@ -283,7 +298,7 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 					o0 = __ffma2_rn(win[0][K - 1 - q], t, o0);
 					o1 = __ffma2_rn(win[1][K - 1 - q], t, o1);
 				}
-				store(zs + p - 2 * R, o0, o1);
+				store(zs + p - 2 * R, y0_of(0), o0, o1);
 			}
 		}
 	}
@@ -579,9 +594,15 @@ int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, i
 			static_cast<int>(smem)), "separable: set shared memory size");
 		separable_fast_kernel<R, true><<<grid, kFThreads, smem, stream>>>(map, a);
 	} else {
-		IANE_GB_CUDA(cudaFuncSetAttribute(separable_fast_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			static_cast<int>(smem)), "separable: set shared memory size");
-		separable_fast_kernel<R, false><<<grid, kFThreads, smem, stream>>>(map, a);
+		auto kernel = separable_fast_kernel<R, false>;
+		IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+			"separable: set shared memory size");
+		// 2-D: blocks stream eight tile rows each (when that still gives several blocks per SM),
+		// so a tile's load overlaps the previous tile's filtering
+		dim3 g2 = grid;
+		const unsigned int streamed = (grid.y + 7) / 8;
+		if (static_cast<long long>(grid.x) * streamed >= 8LL * sms) g2.y = streamed;
+		kernel<<<g2, kFThreads, smem, stream>>>(map, a);
 	}
 	IANE_GB_CUDA(cudaGetLastError(), "separable: launch");
 	return IANE_GB_OK;
