@@ -214,3 +214,38 @@ def test_texture_errors(cuda):
     assert empty.handle == 0
     iane_gb300.convolve(empty.view(), k, empty_like_np((0, 3), np.float32))
     empty.close()
+
+
+# --- single-plane kernels on large images (at least 2 x SMs 64x64 tiles) --------------------
+
+@pytest.mark.parametrize("border", ["clamp", "zero", "mirror"])
+@pytest.mark.parametrize("case", ["f32_tma", "f32_strided", "u8_narrow", "u16_narrow", "i32_copy", "texture_u8",
+                                  "f32_3d_plane_kernel"])
+def test_large_single_plane_parity(cuda, case, border):
+    """Large 2-D images (and a 3-D volume with a one-plane kernel) take the single-plane
+    64x64-tile kernels (direct summation): every staging mode against the oracle."""
+    t = torch()
+    rng = np.random.default_rng(zlib.crc32(repr((case, border)).encode()))
+    shape = (8, 640, 700) if case == "f32_3d_plane_kernel" else (1100, 1500)
+    kshape = (1, 9, 7) if case == "f32_3d_plane_kernel" else (7, 13)
+    kernel = (rng.standard_normal(kshape) / np.prod(kshape)).astype(np.float32)
+    dtype = {"u8_narrow": np.uint8, "texture_u8": np.uint8, "u16_narrow": np.uint16, "i32_copy": np.int32}.get(case,
+                                                                                                        np.float32)
+    src = random_of(rng, dtype, shape)
+    out_dtype = np.float32
+    ref = oracle_conv(src, kernel, out_dtype, border)
+    out = empty_like_np(shape, out_dtype)
+    if case == "texture_u8":
+        tex = iane_gb300.Texture(shape, "uint8").upload(src)
+        source = tex.view()
+    elif case == "f32_strided":
+        big = to_gpu(np.zeros((shape[0], shape[1] + 40), np.float32))
+        big[:, 13:13 + shape[1]] = to_gpu(src)
+        source = big[:, 13:13 + shape[1]]
+    else:
+        source = to_gpu(src)
+    iane_gb300.convolve(source, to_gpu(kernel), out, border)
+    assert_fast_close(to_host(out), ref, src, kernel, border)
+    if case == "texture_u8":
+        tex.close()
+    del t
