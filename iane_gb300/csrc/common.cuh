@@ -205,17 +205,19 @@ __device__ __forceinline__ T texel(cudaTextureObject_t tex, int rank, int x, int
 	return tex3D<T>(tex, x + 0.5f, y + 0.5f, z + 0.5f);
 }
 
-__device__ __forceinline__ double texel_as_double(cudaTextureObject_t tex, int dtype, int rank, int x, int y, int z)
+// A texel as float (exact for the 8- and 16-bit types; i32/u32 round as a float conversion
+// does).
+__device__ __forceinline__ float texel_as_float(cudaTextureObject_t tex, int dtype, int rank, int x, int y, int z)
 {
 	switch (dtype) {
-	case IANE_GB_U8: return static_cast<double>(texel<unsigned char>(tex, rank, x, y, z));
-	case IANE_GB_I8: return static_cast<double>(texel<signed char>(tex, rank, x, y, z));
-	case IANE_GB_U16: return static_cast<double>(texel<unsigned short>(tex, rank, x, y, z));
-	case IANE_GB_I16: return static_cast<double>(texel<short>(tex, rank, x, y, z));
-	case IANE_GB_I32: return static_cast<double>(texel<int>(tex, rank, x, y, z));
-	case IANE_GB_U32: return static_cast<double>(texel<unsigned int>(tex, rank, x, y, z));
-	case IANE_GB_F32: return static_cast<double>(texel<float>(tex, rank, x, y, z));
-	default: return 0.0;
+	case IANE_GB_U8: return static_cast<float>(texel<unsigned char>(tex, rank, x, y, z));
+	case IANE_GB_I8: return static_cast<float>(texel<signed char>(tex, rank, x, y, z));
+	case IANE_GB_U16: return static_cast<float>(texel<unsigned short>(tex, rank, x, y, z));
+	case IANE_GB_I16: return static_cast<float>(texel<short>(tex, rank, x, y, z));
+	case IANE_GB_I32: return static_cast<float>(texel<int>(tex, rank, x, y, z));
+	case IANE_GB_U32: return static_cast<float>(texel<unsigned int>(tex, rank, x, y, z));
+	case IANE_GB_F32: return texel<float>(tex, rank, x, y, z);
+	default: return 0.0f;
 	}
 }
 

@@ -142,8 +142,8 @@ __device__ __forceinline__ void stage_elements(const TileArgs& a, float* dst, in
 				if (zok && map_coord(gx0 + c, a.nx, a.border, xi) && map_coord(gy0 + r, a.ny, a.border, yi)) {
 					in |= 1u << u;
 					if (texture) {
-						raw[u] = __float_as_uint(static_cast<float>(texel_as_double(a.tex.tex, a.tex.dtype, a.tex.rank,
-							a.tex.origin[0] + xi, a.tex.origin[1] + yi, a.tex.origin[2] + zi)));
+						raw[u] = __float_as_uint(texel_as_float(a.tex.tex, a.tex.dtype, a.tex.rank, a.tex.origin[0] + xi,
+							a.tex.origin[1] + yi, a.tex.origin[2] + zi));
 					} else {
 						const char* q = plane + xi * a.s_stride[0] + yi * a.s_stride[1];
 						raw[u] = esize == 1 ? static_cast<uint32_t>(*reinterpret_cast<const uint8_t*>(q))
