@@ -144,6 +144,24 @@ def cpu_sample(observed, psf, threads, iterations):
     return convs * observed.size / dt / 1e9, dt
 
 
+def max_over_ranks(value: float, dist, device) -> float:
+    """The largest of every rank's `value` (the job's time is its slowest replica's); the value
+    itself on a single process."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, units_per_step: float, steps: int, seconds: float) -> float:
+    """Whole-job throughput of `world` replicas that each ran `steps` steps of `units_per_step`
+    units, the slowest taking `seconds`: giga-units per second."""
+    return world * units_per_step * steps / seconds / 1e9
+
+
 def run_reference(args, rank):
     """Reference arm: the reference's CPU RL path (the oracle port: the reference's own build
     needs its headers, which are not on the GPU host), all host threads; each step is one
@@ -688,12 +706,9 @@ def main():
     iane_gb300.device_status()
     step_ms = [a.elapsed_time(b) for a, b in events]
     total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, dev)
     conv_voxels_per_step = 2 * ITERATIONS * VOXELS
-    value = world * conv_voxels_per_step * args.steps / (total_ms / 1e3) / 1e9
+    value = job_throughput(world, conv_voxels_per_step, args.steps, total_ms / 1e3)
     ms_per_step = total_ms / args.steps
 
     # end to end through the C-ABI host entry point
@@ -703,12 +718,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         rl.run_host(obs_host, est_host, ITERATIONS, EPSILON, init=rl.INIT_MEAN, scratch=host_scratch)
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * conv_voxels_per_step * e2e_steps / e2e_s / 1e9
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e_value = job_throughput(world, conv_voxels_per_step, e2e_steps, e2e_s)
 
     with_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
     hbm_legs = measure_hbm_legs(dev, stream, cpu=with_cpu)
