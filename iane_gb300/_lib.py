@@ -55,6 +55,8 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_last_error.restype = ctypes.c_size_t
     l.iane_gb_device_status.argtypes = [vp]
     l.iane_gb_device_status.restype = ctypes.c_int
+    l.iane_gb_wait_probe.argtypes = [ctypes.c_uint, vp]
+    l.iane_gb_wait_probe.restype = ctypes.c_int
     l.iane_gb_convolve.argtypes = [_VIEW_P, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_uint, vp]
     l.iane_gb_convolve.restype = ctypes.c_int
     l.iane_gb_convolve_separable.argtypes = [_VIEW_P, ctypes.POINTER(_VIEW_P), _VIEW_P, ctypes.c_int, vp]

@@ -247,6 +247,21 @@ int iane_gb_device_status(void* stream)
 
 namespace iane_gb {
 
+// A kernel whose one wait never completes: an mbarrier that expects one arrival that nobody
+// makes, waited on with a limit of `limit_ns`; the timeout lands in the status word.
+__global__ void wait_probe_kernel(int* status, unsigned long long limit_ns)
+{
+	__shared__ __align__(8) uint64_t bar;
+	if (threadIdx.x == 0) {
+		mbar_init(&bar, 1);
+		fence_barrier_init();
+	}
+	__syncthreads();
+	if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, limit_ns)) {
+		report_device_status(status, IANE_GB_DEVICE_TIMEOUT);
+	}
+}
+
 int convolve_checked(const DevView& s, const DevView& k, const DevView& d, int border, unsigned flags, void* stream,
 	const TexSource* tex)
 {
@@ -334,6 +349,18 @@ int convolve_checked(const DevView& s, const DevView& k, const DevView& d, int b
 }  // namespace iane_gb
 
 extern "C" {
+
+int iane_gb_wait_probe(unsigned int limit_us, void* stream)
+{
+	if (limit_us == 0 || limit_us > 10000000u) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "wait probe: the limit is 1 us .. 10 s");
+	}
+	int* status = device_status_ptr();
+	if (!status) return IANE_GB_CUDA_ERROR;
+	wait_probe_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(status, 1000ull * limit_us);
+	IANE_GB_CUDA(cudaGetLastError(), "wait probe: launch");
+	return IANE_GB_OK;
+}
 
 int iane_gb_convolve(const iane_gb_view* src, const iane_gb_view* kernel, const iane_gb_view* dst, int border,
 	unsigned flags, void* stream)

@@ -304,13 +304,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 	return done != 0;
 }
 
-// Bounded wait on an mbarrier phase. try_wait suspends for a hardware-chosen interval per
-// call, so the limit corresponds to well over a second. Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ uint64_t global_ns()
 {
-	for (uint32_t i = 0; i < (1u << 24); ++i) {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Bounded wait on an mbarrier phase: gives up (returns false) after `limit_ns` of global time
+// -- two seconds unless told otherwise -- or 2^26 tries, whichever comes first, so that a
+// phase that never completes ends the kernel instead of hanging it. The caller records the
+// timeout in the device status word and finishes.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns = 2000000000ull)
+{
+	if (mbar_try_wait(bar, parity)) {
+		return true;
+	}
+	const uint64_t t0 = global_ns();
+	for (uint32_t i = 1; i < (1u << 26); ++i) {
 		if (mbar_try_wait(bar, parity)) {
 			return true;
+		}
+		if ((i & 255u) == 0 && global_ns() - t0 > limit_ns) {
+			return false;
 		}
 	}
 	return false;

@@ -102,6 +102,12 @@ size_t iane_gb_last_error(char* buf, size_t size);
  * IANE_GB_DEVICE_TIMEOUT if a bounded device-side wait of an earlier launch gave up. */
 int iane_gb_device_status(void* stream);
 
+/* Diagnostic: launch a kernel whose one wait never completes (an mbarrier nobody arrives on),
+ * bounded to `limit_us` microseconds (1 .. 10^7). The kernel records IANE_GB_DEVICE_TIMEOUT in
+ * the status word and ends; the next iane_gb_device_status reports it, and the context stays
+ * usable. Every device-side wait of this library has the same bound (two seconds). */
+int iane_gb_wait_probe(unsigned int limit_us, void* stream);
+
 /*
  * Direct N-D convolution. Replaces iane::convolve for CUDA memory views
  * (reference include/iane/algorithms/convolution.hpp:97-117, with the extent check of

@@ -87,3 +87,9 @@ def test_rl_prepare_rejects_even_psf_without_gpu():
     handle = ctypes.c_void_p()
     assert lib.iane_gb_rl_prepare(ctypes.byref(psf), 2, ext, None, ctypes.byref(handle)) == abi.INVALID_ARGUMENT
     assert not handle.value
+
+
+def test_wait_probe_checks_its_limit_before_any_launch():
+    lib = iane_gb300.lib()
+    for bad in (0, 10000001):
+        assert lib.iane_gb_wait_probe(bad, None) == iane_gb300.abi.INVALID_ARGUMENT
