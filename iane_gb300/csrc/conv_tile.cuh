@@ -175,41 +175,43 @@ __device__ __forceinline__ void stage_elements(const TileArgs& a, float* dst, in
 	}
 }
 
-// kTileTmaNarrow: convert the raw staged box (row pitch `pitch` bytes) into the float tile.
+// kTileTmaNarrow: convert the raw staged box (row pitch `pitch` bytes) into the float tile,
+// four cells at a time: OFF = 16 - RXA and W are multiples of 4, so each group of four is one
+// 4-byte (8-bit types) or 8-byte (16-bit) load from the staging row and one 16-byte store.
 template<int W, int P, int NT, int OFF>
 __device__ __forceinline__ void convert_narrow(const unsigned char* sg, float* t, int H, int pitch, int dtype)
 {
+	static_assert(W % 4 == 0 && OFF % 4 == 0 && P % 4 == 0, "vector conversion");
+	constexpr int G4 = W / 4; // groups of four cells per row
 	const int tid = threadIdx.x;
-	switch (dtype) {
-	case IANE_GB_U8:
-		for (int i = tid; i < W * H; i += NT) {
-			const int r = i / W, c = i - r * W;
-			t[r * P + c] = static_cast<float>(sg[r * pitch + OFF + c]);
+	for (int i = tid; i < G4 * H; i += NT) {
+		const int r = i / G4, g = i - r * G4;
+		float4 v;
+		if (dtype == IANE_GB_U8 || dtype == IANE_GB_I8) {
+			const uint32_t w = *reinterpret_cast<const uint32_t*>(sg + r * pitch + OFF + 4 * g);
+			if (dtype == IANE_GB_U8) {
+				v = make_float4(static_cast<float>(w & 0xffu), static_cast<float>((w >> 8) & 0xffu),
+					static_cast<float>((w >> 16) & 0xffu), static_cast<float>(w >> 24));
+			} else {
+				v = make_float4(static_cast<float>(static_cast<int8_t>(w & 0xffu)),
+					static_cast<float>(static_cast<int8_t>((w >> 8) & 0xffu)),
+					static_cast<float>(static_cast<int8_t>((w >> 16) & 0xffu)), static_cast<float>(static_cast<int8_t>(w >> 24)));
+			}
+		} else {
+			const uint2 w = *reinterpret_cast<const uint2*>(sg + r * pitch + 2 * (OFF + 4 * g));
+			if (dtype == IANE_GB_U16) {
+				v = make_float4(static_cast<float>(w.x & 0xffffu), static_cast<float>(w.x >> 16),
+					static_cast<float>(w.y & 0xffffu), static_cast<float>(w.y >> 16));
+			} else {
+				v = make_float4(static_cast<float>(static_cast<int16_t>(w.x & 0xffffu)),
+					static_cast<float>(static_cast<int16_t>(w.x >> 16)), static_cast<float>(static_cast<int16_t>(w.y & 0xffffu)),
+					static_cast<float>(static_cast<int16_t>(w.y >> 16)));
+			}
 		}
-		break;
-	case IANE_GB_I8:
-		for (int i = tid; i < W * H; i += NT) {
-			const int r = i / W, c = i - r * W;
-			t[r * P + c] = static_cast<float>(static_cast<int8_t>(sg[r * pitch + OFF + c]));
-		}
-		break;
-	case IANE_GB_U16:
-		for (int i = tid; i < W * H; i += NT) {
-			const int r = i / W, c = i - r * W;
-			t[r * P + c] = static_cast<float>(reinterpret_cast<const uint16_t*>(sg + r * pitch)[OFF + c]);
-		}
-		break;
-	default: // IANE_GB_I16
-		for (int i = tid; i < W * H; i += NT) {
-			const int r = i / W, c = i - r * W;
-			t[r * P + c] = static_cast<float>(reinterpret_cast<const int16_t*>(sg + r * pitch)[OFF + c]);
-		}
-		break;
+		*reinterpret_cast<float4*>(t + r * P + 4 * g) = v;
 	}
 }
 
-// One kernel plane's taps applied to a lane's kRY x kRX outputs: `tile` is the lane's corner
-// of the halo tile (pitch P floats), `kplane` the plane's taps (rows of KXP floats).
 template<int KX, int P>
 __device__ __forceinline__ void plane_sums(float (&sum)[kRY][kRX], const float* tile, const float* kplane, int ry, int ky)
 {
