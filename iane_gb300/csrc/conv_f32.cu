@@ -17,6 +17,16 @@ int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevVi
 	if (ky > 63 || src.ext[1] > 65535 * 32 || src.ext[2] > 65535) {
 		return IANE_GB_UNSUPPORTED;
 	}
+	// Small single-plane jobs (too few 64x64 tiles for every SM, and under 5e7 tap-products):
+	// the one-warp blocks of 32x32 tiles are latency-bound there, and the generic kernel (one
+	// output per thread, 256-thread blocks, FP32 sums) with many times the warps per SM is
+	// faster -- measured on GB300: 512^2 7x7 16.5 -> 9.9 us, 256^2 15x15 27.8 -> 8.9 us,
+	// 384x640 11x11 23.5 -> 14.4 us; 1024^2 9x9 (8.5e7) and 512^2 31x31 stay tiled.
+	const long long big_tiles = static_cast<long long>((src.ext[0] + 63) / 64) * ((src.ext[1] + 63) / 64) * src.ext[2];
+	const double work = static_cast<double>(element_count(src)) * kx * ky;
+	if (kz == 1 && big_tiles < 2LL * device_sm_count() && work < 5e7) {
+		return IANE_GB_UNSUPPORTED;
+	}
 	// Shared memory holds one or two kernel planes' taps (ky x 32 floats at most) next to the
 	// halo tiles; the planes stream through it, so kz has no limit here.
 	(void)kz;
