@@ -204,38 +204,40 @@ struct EpiRatioTc {
 		one(x + 32, y, z, p1);
 	}
 
-	// 16 consecutive outputs x0 .. x0 + 15 of row y (x0 a multiple of 16): vector loads and
-	// stores when the run lies inside the image and the observed row is f32 and aligned
-	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&pr)[16]) const
+	// N (8 or 16) consecutive outputs x0 .. x0 + N - 1 of row y (x0 a multiple of N): vector
+	// loads and stores when the run lies inside the image and the observed row is f32 and aligned
+	template<int N>
+	__device__ __forceinline__ void row_n(int x0, int y, int z, const float (&pr)[N]) const
 	{
 		if (y >= ny) return;
 		const char* orow = obs + y * os[1] + z * os[2] + x0 * os[0];
-		if (x0 + 16 <= nx && !obs_u8 && os[0] == 4 && (reinterpret_cast<uintptr_t>(orow) & 15) == 0) {
-			float o[16];
+		if (x0 + N <= nx && !obs_u8 && os[0] == 4 && (reinterpret_cast<uintptr_t>(orow) & 15) == 0) {
+			float o[N];
 #pragma unroll
-			for (int q = 0; q < 4; ++q) {
+			for (int q = 0; q < N / 4; ++q) {
 				const float4 v = *reinterpret_cast<const float4*>(orow + 16 * q);
 				o[4 * q] = v.x;
 				o[4 * q + 1] = v.y;
 				o[4 * q + 2] = v.z;
 				o[4 * q + 3] = v.w;
 			}
-			uint32_t w[8];
+			uint32_t w[N / 2];
 #pragma unroll
-			for (int c = 0; c < 8; ++c) {
+			for (int c = 0; c < N / 2; ++c) {
 				const float r0 = o[2 * c] / (pr[2 * c] > eps ? pr[2 * c] : eps);
 				const float r1 = o[2 * c + 1] / (pr[2 * c + 1] > eps ? pr[2 * c + 1] : eps);
 				const __nv_bfloat162 h = __floats2bfloat162_rn(r0, r1);
 				w[c] = *reinterpret_cast<const uint32_t*>(&h);
 			}
 			uint4* dst = reinterpret_cast<uint4*>(ratio + z * plane + y * pitch + x0);
-			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+#pragma unroll
+			for (int q = 0; q < N / 8; ++q) dst[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
 			return;
 		}
 #pragma unroll
-		for (int c = 0; c < 16; ++c) one(x0 + c, y, z, pr[c]);
+		for (int c = 0; c < N; ++c) one(x0 + c, y, z, pr[c]);
 	}
+	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&pr)[16]) const { row_n<16>(x0, y, z, pr); }
 	__device__ __forceinline__ void finish() const {}
 };
 
@@ -298,32 +300,33 @@ struct EpiUpdateTc {
 		one(x + 32, y, z, c1);
 	}
 
-	// 16 consecutive outputs x0 .. x0 + 15 of row y (x0 a multiple of 16): vector loads and
-	// stores of the estimate and its BF16 shadow when the run lies inside the image
-	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&cv)[16])
+	// N (8 or 16) consecutive outputs x0 .. x0 + N - 1 of row y (x0 a multiple of N): vector
+	// loads and stores of the estimate and its BF16 shadow when the run lies inside the image
+	template<int N>
+	__device__ __forceinline__ void row_n(int x0, int y, int z, const float (&cv)[N])
 	{
 		if (y >= ny) return;
-		if (x0 + 16 > nx || write_out) {
+		if (x0 + N > nx || write_out) {
 #pragma unroll
-			for (int c = 0; c < 16; ++c) one(x0 + c, y, z, cv[c]);
+			for (int c = 0; c < N; ++c) one(x0 + c, y, z, cv[c]);
 			return;
 		}
 		const bool rows_in = y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
-		const bool all_in = rows_in && x0 >= ilo[0] && x0 + 15 <= ihi[0];
+		const bool all_in = rows_in && x0 >= ilo[0] && x0 + N - 1 <= ihi[0];
 		const int cyz = cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
-		float* e = est + z * plane + y * pitch + x0;  // rows are 16-byte aligned, x0 % 16 == 0
-		float old[16];
+		float* e = est + z * plane + y * pitch + x0;  // rows are 16-byte aligned, x0 % 8 == 0
+		float old[N];
 #pragma unroll
-		for (int q = 0; q < 4; ++q) {
+		for (int q = 0; q < N / 4; ++q) {
 			const float4 v = reinterpret_cast<const float4*>(e)[q];
 			old[4 * q] = v.x;
 			old[4 * q + 1] = v.y;
 			old[4 * q + 2] = v.z;
 			old[4 * q + 3] = v.w;
 		}
-		float upd[16];
+		float upd[N];
 #pragma unroll
-		for (int c = 0; c < 16; ++c) {
+		for (int c = 0; c < N; ++c) {
 			float sv = s_interior;
 			if (!all_in && !(rows_in && x0 + c >= ilo[0] && x0 + c <= ihi[0])) sv = sens[cls[x0 + c] + cyz];
 			const float factor = sv > 0.0f ? cv[c] / (sv > eps ? sv : eps) : 0.0f;
@@ -336,19 +339,20 @@ struct EpiUpdateTc {
 			}
 		}
 #pragma unroll
-		for (int q = 0; q < 4; ++q) {
+		for (int q = 0; q < N / 4; ++q) {
 			reinterpret_cast<float4*>(e)[q] = make_float4(upd[4 * q], upd[4 * q + 1], upd[4 * q + 2], upd[4 * q + 3]);
 		}
-		uint32_t w[8];
+		uint32_t w[N / 2];
 #pragma unroll
-		for (int c = 0; c < 8; ++c) {
+		for (int c = 0; c < N / 2; ++c) {
 			const __nv_bfloat162 h = __floats2bfloat162_rn(upd[2 * c], upd[2 * c + 1]);
 			w[c] = *reinterpret_cast<const uint32_t*>(&h);
 		}
 		uint4* d16 = reinterpret_cast<uint4*>(est16 + z * plane16 + y * pitch16 + x0);
-		d16[0] = make_uint4(w[0], w[1], w[2], w[3]);
-		d16[1] = make_uint4(w[4], w[5], w[6], w[7]);
+#pragma unroll
+		for (int q = 0; q < N / 8; ++q) d16[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
 	}
+	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&cv)[16]) { row_n<16>(x0, y, z, cv); }
 
 	__device__ void finish()
 	{

@@ -20,10 +20,11 @@
 // accumulates. All T matrices (ky x 4 x kz KB) are loaded once per CTA by bulk copies; input
 // planes stream through three TMA stages. Warp specialised: one thread of warp 4 issues the
 // loads and MMAs and, once the last input plane reaching output plane i has been issued,
-// commits plane i to its own mbarrier; warps 0-3 (one TMEM lane = one output row each) finish
-// plane i meanwhile -- read its 16 columns and hand each thread's row of 16 voxels to the pass
-// epilogue (EpiRatioTc / EpiUpdateTc row16: vector loads and stores) -- so the epilogue of the
-// early planes overlaps the MMAs of the later ones.
+// commits plane i to its own mbarrier; eight epilogue warps (one TMEM lane = one output row,
+// two warps per lane quarter, each taking 8 of the plane's 16 columns) finish plane i meanwhile
+// -- read its columns and hand each thread's 8 voxels to the pass epilogue (EpiRatioTc /
+// EpiUpdateTc row_n<8>: vector loads and stores) -- so the epilogue of the early planes
+// overlaps the MMAs of the later ones.
 #pragma once
 
 #include "rl_tc.cuh"
@@ -40,7 +41,9 @@ inline size_t tcz_smem_bytes(int ky, int kz)
 {
 	return tcz_tmat_bytes(ky, kz) + kTczStages * tcz_tile_bytes(ky) + (2 * kTczStages + 1 + kTczZ + 1) * 8 + 16;
 }
-constexpr int kTczThreads = 160; // warps 0-3: epilogue (TMEM lanes 0-127), warp 4: loads and MMAs
+// warps 0-3 and 5-8: epilogue, warp w reading TMEM lanes 32 (w % 4) .. + 31 (a warp may only
+// read its own lane quarter) and columns 8 (w > 4) .. + 7 of each plane; warp 4: loads and MMAs
+constexpr int kTczThreads = 288;
 
 __device__ __forceinline__ void tmem_st_zero16(uint32_t taddr)
 {
@@ -167,20 +170,22 @@ __global__ void __launch_bounds__(kTczThreads) tcz_conv_kernel(const __grid_cons
 			}
 		}
 	}
-	// Epilogue (warps 0-3), one output plane at a time as its accumulators become final:
-	// thread t holds row y0 + t's 16 consecutive columns and finishes them with 16-byte loads
-	// and stores.
+	// Epilogue (warps 0-3 and 5-8), one output plane at a time as its accumulators become
+	// final: the thread holds row y0 + 32 (warp % 4) + lane and 8 consecutive columns of it
+	// and finishes them with 16-byte loads and stores.
 	Epi epi = epi_in;
-	if (warp < 4) {
+	if (warp != 4) {
+		const int quarter = warp & 3, half = warp > 4 ? 1 : 0;
+		const uint32_t lanes = static_cast<uint32_t>(32 * quarter) << 16;
 		for (int i = 0; i < nout; ++i) {
 			if (!mbar_wait_bounded(&plane_bar[i], 0)) {
 				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
 			__syncwarp(); // tcgen05.ld is warp-collective
 			tc::fence_after_sync();
-			float v[16];
-			tc::ld_32x32b_x16(tmem + lane_base + 16 * i, v);
-			epi.row16(x0, y0 + tid, Z + i, v);
+			float v[8];
+			tc::ld_32x32b_x8(tmem + lanes + 16 * i + 8 * half, v);
+			epi.template row_n<8>(x0 + 8 * half, y0 + 32 * quarter + lane, Z + i, v);
 		}
 	}
 	tc::fence_before_sync();
