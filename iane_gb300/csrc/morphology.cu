@@ -181,6 +181,77 @@ __global__ void __launch_bounds__(256) morph_box_3d_kernel(DevView src, DevView 
 	}
 }
 
+// Cube footprints of radius R = 1, 2 or 3 in 3-D (the common case), fused like
+// morph_box_3d_kernel but with the scans fully unrolled and each thread's z window in
+// registers: the thread owns the outputs (x0 + tx, y0 + ty + 8 k), k < 4, for every plane of
+// the chunk, and keeps the xy results of the last 2 R + 1 input planes for them. Same scan
+// order as the reference (erosion: z increasing; dilation: decreasing).
+template<class T, bool DILATE, int R>
+__global__ void __launch_bounds__(256) morph_cube_kernel(DevView src, DevView dst, int zc, int border)
+{
+	constexpr int K = 2 * R + 1;
+	constexpr int TW = kTX + 2 * R, TH = kTY + 2 * R;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T* tile = reinterpret_cast<T*>(smem_raw); // TW x TH
+	T* xbuf = tile + TW * TH;                 // 32 x TH
+	const int tx = threadIdx.x, ty = threadIdx.y;
+	const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+	const int z0 = blockIdx.z * zc;
+	const int z1 = min(dst.ext[2], z0 + zc);
+	const int nz = src.ext[2];
+	T win[kTY / 8][K]; // [k][slot], slot K - 1 the newest plane
+#pragma unroll
+	for (int k = 0; k < kTY / 8; ++k)
+#pragma unroll
+		for (int s = 0; s < K; ++s) win[k][s] = start_value<T>(DILATE);
+	for (int zi = z0 - R; zi < z1 + R; ++zi) {
+		int zm = 0;
+		const bool zok = map_coord(zi, nz, border, zm);
+		load_tile<T>(src, tile, x0, y0, R, R, zm, zok, border);
+		__syncthreads();
+#pragma unroll
+		for (int r0 = 0; r0 < TH; r0 += 8) {
+			const int r = r0 + ty;
+			if (r < TH) {
+				const T* row = tile + r * TW + tx;
+				T m = start_value<T>(DILATE);
+#pragma unroll
+				for (int o = 0; o < K; ++o) take<DILATE>(row[DILATE ? 2 * R - o : o], m);
+				xbuf[r * kTX + tx] = m;
+			}
+		}
+		__syncthreads();
+#pragma unroll
+		for (int k = 0; k < kTY / 8; ++k) {
+			const T* col = xbuf + (ty + 8 * k) * kTX + tx;
+			T m = start_value<T>(DILATE);
+#pragma unroll
+			for (int o = 0; o < K; ++o) take<DILATE>(col[(DILATE ? 2 * R - o : o) * kTX], m);
+#pragma unroll
+			for (int s = 0; s < K - 1; ++s) win[k][s] = win[k][s + 1];
+			win[k][K - 1] = m;
+		}
+		const int zo = zi - R; // the output plane whose window ends at zi
+		if (zo >= z0) {
+			const int x = x0 + tx;
+			if (x < dst.ext[0]) {
+#pragma unroll
+				for (int k = 0; k < kTY / 8; ++k) {
+					const int y = y0 + ty + 8 * k;
+					if (y < dst.ext[1]) {
+						T m = start_value<T>(DILATE);
+#pragma unroll
+						for (int o = 0; o < K; ++o) take<DILATE>(win[k][DILATE ? K - 1 - o : o], m);
+						*const_cast<T*>(element_ptr<T>(dst, x, y, zo)) = m;
+					}
+				}
+			}
+		}
+		// the next plane's staging and x pass come after this thread's y pass: both of its
+		// barriers follow every thread's reads of tile and xbuf
+	}
+}
+
 // Box footprint along z (after the xy pass): one output per thread.
 template<class T, bool DILATE>
 __global__ void __launch_bounds__(256) morph_box_z_kernel(DevView src, DevView dst, int rz, int border)
@@ -256,6 +327,23 @@ int launch_op(const DevView& s, const DevView& d, const int* r, const uint8_t* m
 	const dim3 gt((d.ext[0] + kTX - 1) / kTX, (d.ext[1] + kTY - 1) / kTY, d.ext[2]);
 	if (r[2] == 0) {
 		xy<<<gt, dim3(32, 8), smem, st>>>(s, d, r[0], r[1], border);
+		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
+		return IANE_GB_OK;
+	}
+	if (r[0] == r[1] && r[1] == r[2] && r[0] >= 1 && r[0] <= 3) {
+		// cube footprint: the unrolled kernel with the z window in registers
+		const long long tiles = static_cast<long long>(gt.x) * gt.y;
+		int zc = 32;
+		while (zc > 4 && tiles * ((d.ext[2] + zc - 1) / zc) < 8LL * device_sm_count()) zc /= 2;
+		const dim3 g3(gt.x, gt.y, (d.ext[2] + zc - 1) / zc);
+		const size_t sm = box_xy_smem(r[0], r[0], sizeof(T));
+		if (r[0] == 1) {
+			morph_cube_kernel<T, DILATE, 1><<<g3, dim3(32, 8), sm, st>>>(s, d, zc, border);
+		} else if (r[0] == 2) {
+			morph_cube_kernel<T, DILATE, 2><<<g3, dim3(32, 8), sm, st>>>(s, d, zc, border);
+		} else {
+			morph_cube_kernel<T, DILATE, 3><<<g3, dim3(32, 8), sm, st>>>(s, d, zc, border);
+		}
 		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
 		return IANE_GB_OK;
 	}

@@ -114,3 +114,26 @@ def test_errors(cuda):
     assert info.value.status == iane_gb300.abi.UNSUPPORTED
     with pytest.raises(iane_gb300.IaneError):
         iane_gb300.morphology(to_gpu(np.zeros((8, 8), np.float32)).bfloat16(), a.clone().bfloat16(), (1, 1))
+
+
+@pytest.mark.parametrize("radius", [1, 2, 3])
+@pytest.mark.parametrize("dtype", [np.uint8, np.int16, np.uint32, np.float32, np.float64], ids=lambda d: np.dtype(d).name)
+def test_cube_footprints(cuda, dtype, radius):
+    """Equal radii on all three axes take the unrolled kernel with the z window in registers;
+    several z chunks (the volume is deeper than one chunk), NaN and signed zeros included."""
+    rng = np.random.default_rng(zlib.crc32(repr((np.dtype(dtype).name, radius)).encode()))
+    shape = (45, 37, 70)
+    if np.issubdtype(dtype, np.floating):
+        src = rng.standard_normal(shape).astype(dtype)
+        src[rng.random(shape) < 0.05] = np.nan
+        src[rng.random(shape) < 0.05] = 0.0
+        src[rng.random(shape) < 0.05] = -0.0
+    else:
+        info = np.iinfo(dtype)
+        src = rng.integers(info.min, info.max, shape, dtype=dtype, endpoint=True)
+    r = (radius,) * 3
+    for op in ("erode", "dilate"):
+        for border in ("clamp", "zero", "mirror"):
+            ref = np.zeros_like(src)
+            oracle.morphology(src, ref, r, op, border)
+            assert run_gpu(src, r, op, border).tobytes() == ref.tobytes(), (op, border)
