@@ -93,3 +93,60 @@ def test_wait_probe_checks_its_limit_before_any_launch():
     lib = iane_gb300.lib()
     for bad in (0, 10000001):
         assert lib.iane_gb_wait_probe(bad, None) == iane_gb300.abi.INVALID_ARGUMENT
+
+
+def test_rgb8_and_texture_argument_checks():
+    lib = _lib.lib()
+    rgb = np.zeros((4, 5, 3), np.uint8)
+    s = abi.rgb8_view(rgb.ctypes.data, rgb.shape, rgb.strides)
+    plain = np.zeros((4, 5), np.uint8)
+    k = _host_view(np.ones((3, 3), np.float32))
+    d = _host_view(plain)
+    # rgb8 needs an rgb8 destination
+    assert lib.iane_gb_convolve(ctypes.byref(s), ctypes.byref(k), ctypes.byref(d), 0, 0, None) == abi.UNSUPPORTED
+    # texture creation: texel types and ranks; an empty texture needs no device
+    handle = ctypes.c_uint64(7)
+    ext = (ctypes.c_int32 * 3)(4, 4, 1)
+    assert lib.iane_gb_texture_create(abi.F64, 2, ext, ctypes.byref(handle)) == abi.UNSUPPORTED
+    assert lib.iane_gb_texture_create(abi.F32, 4, ext, ctypes.byref(handle)) == abi.UNSUPPORTED
+    neg = (ctypes.c_int32 * 3)(4, -1, 1)
+    assert lib.iane_gb_texture_create(abi.F32, 2, neg, ctypes.byref(handle)) == abi.INVALID_ARGUMENT
+    empty = (ctypes.c_int32 * 3)(0, 4, 1)
+    assert lib.iane_gb_texture_create(abi.U8, 2, empty, ctypes.byref(handle)) == abi.OK
+    assert handle.value == 0
+    assert lib.iane_gb_texture_destroy(0) == abi.OK
+    assert lib.iane_gb_convolve_texture(None, ctypes.byref(k), ctypes.byref(d), 0, 0, None) == abi.INVALID_ARGUMENT
+    assert lib.iane_gb_texture_upload(12345, ctypes.byref(d), None) == abi.INVALID_ARGUMENT
+
+
+def test_morphology_argument_checks():
+    lib = _lib.lib()
+    a = np.zeros((6, 7), np.float32)
+    s, d = _host_view(a), _host_view(a.copy())
+    bad = (ctypes.c_int32 * 3)(-1, 1, 0)
+    assert lib.iane_gb_morphology(ctypes.byref(s), ctypes.byref(d), bad, None, abi.ERODE, 0, None) == abi.INVALID_ARGUMENT
+    ok = (ctypes.c_int32 * 3)(1, 1, 0)
+    assert lib.iane_gb_morphology(ctypes.byref(s), ctypes.byref(d), ok, None, 7, 0, None) == abi.INVALID_ARGUMENT
+    assert lib.iane_gb_morphology(ctypes.byref(s), ctypes.byref(d), ok, None, abi.OPENING, 0, None) == \
+        abi.INVALID_ARGUMENT
+    other = _host_view(np.zeros((6, 7), np.float64))
+    assert lib.iane_gb_morphology(ctypes.byref(s), ctypes.byref(other), ok, None, abi.ERODE, 0, None) == \
+        abi.INVALID_ARGUMENT
+    ext = (ctypes.c_int32 * 3)(7, 6, 1)
+    assert lib.iane_gb_morphology_scratch_bytes(abi.F32, 2, ext) == 2 * ((7 * 6 * 4 + 255) // 256 * 256)
+
+
+def test_wiener_argument_checks():
+    lib = _lib.lib()
+    psf = _host_view(np.ones((3, 3), np.float32))
+    ext = (ctypes.c_int32 * 3)(16, 16, 1)
+    plan = ctypes.c_void_p()
+    for noise in (0.0, -1.0, float("nan"), float("inf")):
+        assert lib.iane_gb_wiener_prepare(ctypes.byref(psf), 2, ext, noise, None, ctypes.byref(plan)) == \
+            abi.INVALID_ARGUMENT
+        assert "Noise must be finite and positive" in _lib.last_error()
+    small = (ctypes.c_int32 * 3)(2, 16, 1)
+    assert lib.iane_gb_wiener_prepare(ctypes.byref(psf), 2, small, 0.01, None, ctypes.byref(plan)) == \
+        abi.INVALID_ARGUMENT
+    assert "PSF must fit inside the input image" in _lib.last_error()
+    assert lib.iane_gb_wiener_run(None, None, None, None, 0, None) == abi.INVALID_ARGUMENT
