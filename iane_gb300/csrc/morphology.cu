@@ -182,15 +182,21 @@ __global__ void __launch_bounds__(256) morph_box_3d_kernel(DevView src, DevView 
 }
 
 // Cube footprints of radius R = 1, 2 or 3 in 3-D (the common case), fused like
-// morph_box_3d_kernel but with the scans fully unrolled and each thread's z window in
-// registers: the thread owns the outputs (x0 + tx, y0 + ty + 8 k), k < 4, for every plane of
-// the chunk, and keeps the xy results of the last 2 R + 1 input planes for them. Same scan
-// order as the reference (erosion: z increasing; dilation: decreasing).
+// morph_box_3d_kernel with the scans fully unrolled. Thread (tx, ty) owns the outputs
+// (x0 + tx, y0 + 4 ty + k), k < 4, of every plane of the chunk and keeps the xy results of the
+// last 2 R + 1 input planes for them in registers. It stages the same cells (rows ty + 8 i,
+// columns tx + 32 j) of every input plane, so their in-plane byte offsets and border rule are
+// worked out once per block, and the next plane's cells are loaded into registers while the
+// current plane is scanned. Same scan order as the reference (erosion: x, y and z increasing;
+// dilation: decreasing).
 template<class T, bool DILATE, int R>
-__global__ void __launch_bounds__(256) morph_cube_kernel(DevView src, DevView dst, int zc, int border)
+__global__ void __launch_bounds__(256, sizeof(T) == 8 || R == 3 ? 2 : 3) morph_cube_kernel(DevView src, DevView dst, int zc, int border)
 {
 	constexpr int K = 2 * R + 1;
 	constexpr int TW = kTX + 2 * R, TH = kTY + 2 * R;
+	constexpr int NR = (TH + 7) / 8;   // staged rows per thread
+	constexpr int NC = (TW + 31) / 32; // staged columns per thread
+	constexpr int OY = kTY / 8;        // consecutive output rows per thread
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T* tile = reinterpret_cast<T*>(smem_raw); // TW x TH
 	T* xbuf = tile + TW * TH;                 // 32 x TH
@@ -199,19 +205,58 @@ __global__ void __launch_bounds__(256) morph_cube_kernel(DevView src, DevView ds
 	const int z0 = blockIdx.z * zc;
 	const int z1 = min(dst.ext[2], z0 + zc);
 	const int nz = src.ext[2];
-	T win[kTY / 8][K]; // [k][slot], slot K - 1 the newest plane
+
+	// In-plane byte offsets of the staged cells (32-bit: the launcher sends views whose plane
+	// spans more than 2^31 bytes elsewhere); bit i * NC + j of `live` marks a cell that holds a
+	// sample (a cell of the tile with its bit clear is a zero-border 0)
+	int coff[NC], roff[NR];
+	unsigned xlive = 0, live = 0;
 #pragma unroll
-	for (int k = 0; k < kTY / 8; ++k)
+	for (int j = 0; j < NC; ++j) {
+		int xi = 0;
+		if (tx + 32 * j < TW && map_coord(x0 - R + tx + 32 * j, src.ext[0], border, xi)) xlive |= 1u << j;
+		coff[j] = xi * static_cast<int>(src.stride[0]);
+	}
 #pragma unroll
-		for (int s = 0; s < K; ++s) win[k][s] = start_value<T>(DILATE);
-	for (int zi = z0 - R; zi < z1 + R; ++zi) {
+	for (int i = 0; i < NR; ++i) {
+		int yi = 0;
+		if (ty + 8 * i < TH && map_coord(y0 - R + ty + 8 * i, src.ext[1], border, yi)) live |= xlive << (i * NC);
+		roff[i] = yi * static_cast<int>(src.stride[1]);
+	}
+	T cell[NR][NC];
+	auto fetch = [&](int zi) {
 		int zm = 0;
 		const bool zok = map_coord(zi, nz, border, zm);
-		load_tile<T>(src, tile, x0, y0, R, R, zm, zok, border);
+		const char* base = src.ptr + static_cast<long long>(zm) * src.stride[2];
+#pragma unroll
+		for (int i = 0; i < NR; ++i)
+#pragma unroll
+			for (int j = 0; j < NC; ++j)
+				cell[i][j] = zok && (live >> (i * NC + j) & 1u) ? *reinterpret_cast<const T*>(base + (roff[i] + coff[j])) : T(0);
+	};
+
+	const int x = x0 + tx;
+	const int yb = y0 + OY * ty;
+	const int rows_out = x < dst.ext[0] ? min(OY, dst.ext[1] - yb) : 0;
+	const int out_row = static_cast<int>(dst.stride[1]);
+	char* const out_base = dst.ptr + (rows_out > 0 ? x * static_cast<int>(dst.stride[0]) + yb * out_row : 0);
+	T win[OY][K]; // [k][slot], slot K - 1 the newest plane
+#pragma unroll
+	for (int k = 0; k < OY; ++k)
+#pragma unroll
+		for (int s = 0; s < K; ++s) win[k][s] = start_value<T>(DILATE);
+	fetch(z0 - R);
+	for (int zi = z0 - R; zi < z1 + R; ++zi) {
+#pragma unroll
+		for (int i = 0; i < NR; ++i)
+#pragma unroll
+			for (int j = 0; j < NC; ++j)
+				if (ty + 8 * i < TH && tx + 32 * j < TW) tile[(ty + 8 * i) * TW + tx + 32 * j] = cell[i][j];
+		if (zi + 1 < z1 + R) fetch(zi + 1); // in flight while this plane is scanned
 		__syncthreads();
 #pragma unroll
-		for (int r0 = 0; r0 < TH; r0 += 8) {
-			const int r = r0 + ty;
+		for (int i = 0; i < NR; ++i) {
+			const int r = ty + 8 * i;
 			if (r < TH) {
 				const T* row = tile + r * TW + tx;
 				T m = start_value<T>(DILATE);
@@ -221,29 +266,28 @@ __global__ void __launch_bounds__(256) morph_cube_kernel(DevView src, DevView ds
 			}
 		}
 		__syncthreads();
+		T col[OY + 2 * R];
 #pragma unroll
-		for (int k = 0; k < kTY / 8; ++k) {
-			const T* col = xbuf + (ty + 8 * k) * kTX + tx;
+		for (int q = 0; q < OY + 2 * R; ++q) col[q] = xbuf[(OY * ty + q) * kTX + tx];
+#pragma unroll
+		for (int k = 0; k < OY; ++k) {
 			T m = start_value<T>(DILATE);
 #pragma unroll
-			for (int o = 0; o < K; ++o) take<DILATE>(col[(DILATE ? 2 * R - o : o) * kTX], m);
+			for (int o = 0; o < K; ++o) take<DILATE>(col[k + (DILATE ? 2 * R - o : o)], m);
 #pragma unroll
 			for (int s = 0; s < K - 1; ++s) win[k][s] = win[k][s + 1];
 			win[k][K - 1] = m;
 		}
 		const int zo = zi - R; // the output plane whose window ends at zi
 		if (zo >= z0) {
-			const int x = x0 + tx;
-			if (x < dst.ext[0]) {
+			char* const out = out_base + static_cast<long long>(zo) * dst.stride[2];
 #pragma unroll
-				for (int k = 0; k < kTY / 8; ++k) {
-					const int y = y0 + ty + 8 * k;
-					if (y < dst.ext[1]) {
-						T m = start_value<T>(DILATE);
+			for (int k = 0; k < OY; ++k) {
+				if (k < rows_out) {
+					T m = start_value<T>(DILATE);
 #pragma unroll
-						for (int o = 0; o < K; ++o) take<DILATE>(win[k][DILATE ? K - 1 - o : o], m);
-						*const_cast<T*>(element_ptr<T>(dst, x, y, zo)) = m;
-					}
+					for (int o = 0; o < K; ++o) take<DILATE>(win[k][DILATE ? K - 1 - o : o], m);
+					*reinterpret_cast<T*>(out + k * out_row) = m;
 				}
 			}
 		}
@@ -295,6 +339,20 @@ __global__ void __launch_bounds__(256) morph_direct_kernel(DevView src, DevView 
 	*const_cast<T*>(element_ptr<T>(dst, x, y, z)) = m;
 }
 
+// Whether every in-plane byte offset of the view fits in an int (the cube kernel's offsets).
+bool plane_offsets_fit(const DevView& v)
+{
+	constexpr long long kMax = std::numeric_limits<int>::max();
+	long long span = 0;
+	for (int a = 0; a < 2; ++a) {
+		if (v.ext[a] <= 1) continue;
+		const long long st = v.stride[a] < 0 ? -v.stride[a] : v.stride[a];
+		if (st > kMax) return false;
+		span += static_cast<long long>(v.ext[a] - 1) * st;
+	}
+	return span <= kMax;
+}
+
 size_t box_xy_smem(int rx, int ry, int esize)
 {
 	return static_cast<size_t>((kTX + 2 * rx) * (kTY + 2 * ry) + kTX * (kTY + 2 * ry)) * esize;
@@ -330,7 +388,7 @@ int launch_op(const DevView& s, const DevView& d, const int* r, const uint8_t* m
 		IANE_GB_CUDA(cudaGetLastError(), "morphology: launch");
 		return IANE_GB_OK;
 	}
-	if (r[0] == r[1] && r[1] == r[2] && r[0] >= 1 && r[0] <= 3) {
+	if (r[0] == r[1] && r[1] == r[2] && r[0] >= 1 && r[0] <= 3 && plane_offsets_fit(s) && plane_offsets_fit(d)) {
 		// cube footprint: the unrolled kernel with the z window in registers
 		const long long tiles = static_cast<long long>(gt.x) * gt.y;
 		int zc = 32;

@@ -137,3 +137,43 @@ def test_cube_footprints(cuda, dtype, radius):
             ref = np.zeros_like(src)
             oracle.morphology(src, ref, r, op, border)
             assert run_gpu(src, r, op, border).tobytes() == ref.tobytes(), (op, border)
+
+
+@pytest.mark.parametrize("radius", [1, 2, 3])
+def test_cube_footprints_on_strided_views(cuda, radius):
+    """The cube kernel's per-block staging offsets on a cropped view with an x stride of two
+    elements, all three borders."""
+    t = torch()
+    rng = np.random.default_rng(100 + radius)
+    big = rng.standard_normal((44, 33, 140)).astype(np.float32)
+    big[rng.random(big.shape) < 0.03] = np.nan
+    crop = (slice(2, 40), slice(3, 30), slice(1, 130, 2))
+    src = np.ascontiguousarray(big[crop])
+    g = to_gpu(big)
+    r = (radius,) * 3
+    for op in ("erode", "dilate"):
+        for border in ("clamp", "zero", "mirror"):
+            ref = np.zeros_like(src)
+            oracle.morphology(src, ref, r, op, border)
+            out = t.zeros((44, 33, 140), dtype=t.float32, device="cuda")
+            iane_gb300.morphology(g[crop], out[crop], r, op, border)
+            assert to_host(out[crop]).tobytes() == ref.tobytes(), (op, border)
+
+
+def test_cube_footprint_with_a_plane_beyond_31_bit_offsets(cuda):
+    """A view whose plane spans more than 2^31 bytes (two rows 2^31 + 4 KiB apart) takes the
+    general fused 3-D kernel; the result is the same."""
+    t = torch()
+    row = (1 << 29) + 1024  # elements between the two rows: 2^31 + 4 KiB
+    buf = t.zeros(row + 3 * 64 + 64, dtype=t.float32, device="cuda")
+    rng = np.random.default_rng(7)
+    vals = rng.standard_normal((3, 2, 64)).astype(np.float32)
+    view = buf.as_strided((3, 2, 64), (64, row, 1))
+    view.copy_(t.from_numpy(vals).cuda())
+    out = t.zeros((3, 2, 64), dtype=t.float32, device="cuda")
+    for op in ("erode", "dilate"):
+        ref = np.zeros_like(vals)
+        oracle.morphology(vals, ref, (1, 1, 1), op, "clamp")
+        iane_gb300.morphology(view, out, (1, 1, 1), op, "clamp")
+        assert to_host(out).tobytes() == ref.tobytes(), op
+    del buf
