@@ -181,58 +181,101 @@ __global__ void __launch_bounds__(256) morph_box_3d_kernel(DevView src, DevView 
 	}
 }
 
+// The y pass of the cube kernel for one thread's OY consecutive outputs: col[q] is the x-pass
+// result of tile row OY * ty + q, and output k takes rows k .. k + 2 R in the reference's order
+// (increasing for erosion, decreasing for dilation). For 2 R >= OY every window holds rows OY - 1
+// and OY, so it splits there into a part inside rows [0, OY) and a part inside [OY, k + 2 R];
+// the two parts' first extremes are running values shared by the outputs, and combining them
+// in scan order gives the first extreme of the whole window (the reference's `value < result`
+// rule is associative over consecutive runs of the scan). Erosion scans the lower part first,
+// so its partials are extended towards lower rows keeping ties (<=) and the upper partial
+// towards higher rows replacing only on <; dilation mirrors this (upper part first, extended
+// towards higher rows keeping ties (>=), lower part replacing only on >).
+template<class T, bool DILATE, int R, int OY>
+__device__ __forceinline__ void cube_y_pass(const T (&col)[OY + 2 * R], T (&m)[OY])
+{
+	if constexpr (2 * R >= OY) {
+		T part[OY];
+		T run = start_value<T>(DILATE);
+#pragma unroll
+		for (int k = OY - 1; k >= 0; --k) {
+			const T v = col[k];
+			if (DILATE ? v > run : v <= run) run = v;
+			part[k] = run;
+		}
+		T edge = start_value<T>(DILATE);
+#pragma unroll
+		for (int j = OY; j < OY + 2 * R; ++j) {
+			const T v = col[j];
+			if (DILATE ? v >= edge : v < edge) edge = v;
+			const int k = j - 2 * R;
+			if (k >= 0) {
+				if constexpr (DILATE) {
+					m[k] = part[k] > edge ? part[k] : edge;
+				} else {
+					m[k] = edge < part[k] ? edge : part[k];
+				}
+			}
+		}
+	} else {
+#pragma unroll
+		for (int k = 0; k < OY; ++k) {
+			T v = start_value<T>(DILATE);
+#pragma unroll
+			for (int o = 0; o <= 2 * R; ++o) take<DILATE>(col[k + (DILATE ? 2 * R - o : o)], v);
+			m[k] = v;
+		}
+	}
+}
+
 // Cube footprints of radius R = 1, 2 or 3 in 3-D (the common case), fused like
 // morph_box_3d_kernel with the scans fully unrolled. Thread (tx, ty) owns the outputs
 // (x0 + tx, y0 + 4 ty + k), k < 4, of every plane of the chunk and keeps the xy results of the
-// last 2 R + 1 input planes for them in registers. It stages the same cells (rows ty + 8 i,
-// columns tx + 32 j) of every input plane, so their in-plane byte offsets and border rule are
-// worked out once per block, and the next plane's cells are loaded into registers while the
-// current plane is scanned. Same scan order as the reference (erosion: x, y and z increasing;
-// dilation: decreasing).
+// last 2 R + 1 input planes for them in registers. The 256 threads stage the tile's cells
+// linearly (cell tid + 256 m), the same cells in every input plane, so their in-plane byte
+// offsets and border rule are worked out once per block, and the next plane's cells are
+// loaded into registers while the current plane is scanned. Same scan order as the reference
+// (erosion: x, y and z increasing; dilation: decreasing).
 template<class T, bool DILATE, int R>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 || R == 3 ? 2 : 3) morph_cube_kernel(DevView src, DevView dst, int zc, int border)
 {
 	constexpr int K = 2 * R + 1;
 	constexpr int TW = kTX + 2 * R, TH = kTY + 2 * R;
-	constexpr int NR = (TH + 7) / 8;   // staged rows per thread
-	constexpr int NC = (TW + 31) / 32; // staged columns per thread
-	constexpr int OY = kTY / 8;        // consecutive output rows per thread
+	constexpr int NCELL = TW * TH;
+	constexpr int M = (NCELL + 255) / 256; // staged cells per thread
+	constexpr int OY = kTY / 8;            // consecutive output rows per thread
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T* tile = reinterpret_cast<T*>(smem_raw); // TW x TH
-	T* xbuf = tile + TW * TH;                 // 32 x TH
+	T* xbuf = tile + NCELL;                   // 32 x TH
 	const int tx = threadIdx.x, ty = threadIdx.y;
+	const int tid = ty * 32 + tx;
 	const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
 	const int z0 = blockIdx.z * zc;
 	const int z1 = min(dst.ext[2], z0 + zc);
 	const int nz = src.ext[2];
 
 	// In-plane byte offsets of the staged cells (32-bit: the launcher sends views whose plane
-	// spans more than 2^31 bytes elsewhere); bit i * NC + j of `live` marks a cell that holds a
-	// sample (a cell of the tile with its bit clear is a zero-border 0)
-	int coff[NC], roff[NR];
-	unsigned xlive = 0, live = 0;
+	// spans more than 2^31 bytes elsewhere); bit m of `live` marks a cell that holds a sample
+	// (a cell of the tile with its bit clear is a zero-border 0)
+	int off[M];
+	unsigned live = 0;
 #pragma unroll
-	for (int j = 0; j < NC; ++j) {
-		int xi = 0;
-		if (tx + 32 * j < TW && map_coord(x0 - R + tx + 32 * j, src.ext[0], border, xi)) xlive |= 1u << j;
-		coff[j] = xi * static_cast<int>(src.stride[0]);
+	for (int m = 0; m < M; ++m) {
+		const int c = tid + 256 * m;
+		const int r = c / TW, q = c - r * TW;
+		int xi = 0, yi = 0;
+		if (c < NCELL && map_coord(x0 - R + q, src.ext[0], border, xi) && map_coord(y0 - R + r, src.ext[1], border, yi)) {
+			live |= 1u << m;
+		}
+		off[m] = xi * static_cast<int>(src.stride[0]) + yi * static_cast<int>(src.stride[1]);
 	}
-#pragma unroll
-	for (int i = 0; i < NR; ++i) {
-		int yi = 0;
-		if (ty + 8 * i < TH && map_coord(y0 - R + ty + 8 * i, src.ext[1], border, yi)) live |= xlive << (i * NC);
-		roff[i] = yi * static_cast<int>(src.stride[1]);
-	}
-	T cell[NR][NC];
+	T cell[M];
 	auto fetch = [&](int zi) {
 		int zm = 0;
 		const bool zok = map_coord(zi, nz, border, zm);
 		const char* base = src.ptr + static_cast<long long>(zm) * src.stride[2];
 #pragma unroll
-		for (int i = 0; i < NR; ++i)
-#pragma unroll
-			for (int j = 0; j < NC; ++j)
-				cell[i][j] = zok && (live >> (i * NC + j) & 1u) ? *reinterpret_cast<const T*>(base + (roff[i] + coff[j])) : T(0);
+		for (int m = 0; m < M; ++m) cell[m] = zok && (live >> m & 1u) ? *reinterpret_cast<const T*>(base + off[m]) : T(0);
 	};
 
 	const int x = x0 + tx;
@@ -248,35 +291,33 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 || R == 3 ? 2 : 3) morph_c
 	fetch(z0 - R);
 	for (int zi = z0 - R; zi < z1 + R; ++zi) {
 #pragma unroll
-		for (int i = 0; i < NR; ++i)
-#pragma unroll
-			for (int j = 0; j < NC; ++j)
-				if (ty + 8 * i < TH && tx + 32 * j < TW) tile[(ty + 8 * i) * TW + tx + 32 * j] = cell[i][j];
+		for (int m = 0; m < M; ++m) {
+			if (m + 1 < M || tid + 256 * m < NCELL) tile[tid + 256 * m] = cell[m];
+		}
 		if (zi + 1 < z1 + R) fetch(zi + 1); // in flight while this plane is scanned
 		__syncthreads();
 #pragma unroll
-		for (int i = 0; i < NR; ++i) {
+		for (int i = 0; i < (TH + 7) / 8; ++i) {
 			const int r = ty + 8 * i;
 			if (r < TH) {
 				const T* row = tile + r * TW + tx;
-				T m = start_value<T>(DILATE);
+				T v = start_value<T>(DILATE);
 #pragma unroll
-				for (int o = 0; o < K; ++o) take<DILATE>(row[DILATE ? 2 * R - o : o], m);
-				xbuf[r * kTX + tx] = m;
+				for (int o = 0; o < K; ++o) take<DILATE>(row[DILATE ? 2 * R - o : o], v);
+				xbuf[r * kTX + tx] = v;
 			}
 		}
 		__syncthreads();
 		T col[OY + 2 * R];
 #pragma unroll
 		for (int q = 0; q < OY + 2 * R; ++q) col[q] = xbuf[(OY * ty + q) * kTX + tx];
+		T ym[OY];
+		cube_y_pass<T, DILATE, R, OY>(col, ym);
 #pragma unroll
 		for (int k = 0; k < OY; ++k) {
-			T m = start_value<T>(DILATE);
-#pragma unroll
-			for (int o = 0; o < K; ++o) take<DILATE>(col[k + (DILATE ? 2 * R - o : o)], m);
 #pragma unroll
 			for (int s = 0; s < K - 1; ++s) win[k][s] = win[k][s + 1];
-			win[k][K - 1] = m;
+			win[k][K - 1] = ym[k];
 		}
 		const int zo = zi - R; // the output plane whose window ends at zi
 		if (zo >= z0) {
@@ -284,10 +325,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 || R == 3 ? 2 : 3) morph_c
 #pragma unroll
 			for (int k = 0; k < OY; ++k) {
 				if (k < rows_out) {
-					T m = start_value<T>(DILATE);
+					T v = start_value<T>(DILATE);
 #pragma unroll
-					for (int o = 0; o < K; ++o) take<DILATE>(win[k][DILATE ? K - 1 - o : o], m);
-					*reinterpret_cast<T*>(out + k * out_row) = m;
+					for (int o = 0; o < K; ++o) take<DILATE>(win[k][DILATE ? K - 1 - o : o], v);
+					*reinterpret_cast<T*>(out + k * out_row) = v;
 				}
 			}
 		}
