@@ -132,6 +132,29 @@ def recorded_traffic():
     return None
 
 
+_FP32_PEAK = {}
+
+
+def fp32_peak_tflops(dev):
+    """The FP32 FMA ceiling of this GPU, measured by the library's probe (independent FMA
+    chains on every lane; scalar FFMA and the packed two-lane form), with the nominal figure
+    from the SM count and the maximum clock beside it. Measured once per process."""
+    if "peak" not in _FP32_PEAK:
+        import torch
+
+        import iane_gb300
+
+        with torch.cuda.device(dev):
+            scalar = iane_gb300.fp32_peak(paired=False)
+            paired = iane_gb300.fp32_peak(paired=True)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peaks, _ = measured_peaks()
+        nominal = sms * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+        _FP32_PEAK.update({"peak": max(scalar, paired), "scalar_ffma": scalar, "paired_ffma2": paired,
+                           "nominal": nominal, "sms": sms})
+    return _FP32_PEAK
+
+
 def cpu_sample(observed, psf, threads, iterations):
     """The reference's RL loop (oracle port, all host threads) over the full volume: the
     sensitivity convolution plus `iterations` iterations of two convolutions each."""
@@ -308,12 +331,14 @@ def measure_hbm_legs(dev, stream, reps=20, cpu=True):
     return out
 
 
-def measure_bf16_leg(dev, stream, reps=5):
+def measure_bf16_leg(dev, stream, reps=5, cpu=True):
     """The 3-D RL precision path: 256x256x64, PSF 9x9x9 sigma 2.5, 50 iterations, BF16
     images and PSF in tcgen05 implicit-GEMM convolutions (FP32 accumulation), beside the
-    FP32 SIMT path on the same input. Error of the BF16 result is reported against the
-    FP32 path's result (the FP32 path itself is within 1e-6 rel-L2 of the FP64-accumulating
-    CPU oracle per the tests)."""
+    FP32 SIMT path on the same input. With `cpu`, the CPU baseline of this configuration is
+    the reference's RL loop (the oracle port: FP64-accumulated convolutions, all host
+    threads) run for all 50 iterations on the same input, and both GPU results state their
+    max-abs and relative-L2 error against it."""
+    import numpy as np
     import torch
 
     import iane_gb300
@@ -355,6 +380,24 @@ def measure_bf16_leg(dev, stream, reps=5):
     d = results["bf16"] - results["f32"]
     out["bf16_vs_f32"] = {"rel_l2": float(d.norm() / results["f32"].norm()), "max_abs": float(d.abs().max()),
                           "speedup": out["f32"]["ms_per_run"] / out["bf16"]["ms_per_run"]}
+    if cpu:
+        import oracle
+        from oracle import build as oracle_build
+
+        oracle_build.build_oracle()
+        threads = oracle.default_threads()
+        t0 = time.perf_counter()
+        ref = oracle.rl(observed, psf, ITERATIONS, EPSILON, init=oracle.abi.RL_INIT_MEAN, threads=threads)
+        dt = time.perf_counter() - t0
+        ref64 = torch.from_numpy(ref.astype(np.float64)).to(dev)
+        for precision in ("bf16", "f32"):
+            e = results[precision] - ref64
+            out[precision]["vs_fp64_oracle"] = {"rel_l2": float(e.norm() / ref64.norm()),
+                                                "max_abs": float(e.abs().max()),
+                                                "max_abs_rel_to_max": float(e.abs().max() / ref64.abs().max())}
+        out["cpu_baseline"] = {"value": 2 * ITERATIONS * observed.size / dt / 1e9, "unit": UNIT, "cores": threads,
+                               "kind": "port", "sample": f"oracle RL (FP64-accumulated convolutions), all "
+                                                         f"{ITERATIONS} iterations on the full volume ({dt:.1f} s)"}
     out["config"] = "256x256x64, PSF 9x9x9 sigma 2.5, 50 iterations, flat start"
     return out
 
@@ -401,7 +444,7 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     assert all(bool(torch.isfinite(o).all()) for o in outs)
     peaks, _ = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    fp32 = 152 * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    fp32 = fp32_peak_tflops(dev)["peak"]
     alg_bytes = 24.0 * pixels * iterations   # per iteration: pass A 12 B/px, pass B 12 B/px
     res = {"images": len(obs), "pixels": pixels, "iterations": iterations, "ms_per_run": ms,
            "gvoxel_s": 2 * iterations * pixels / (ms / 1e3) / 1e9, "tflops_useful": 2 * macs / (ms / 1e3) / 1e12,
@@ -680,6 +723,7 @@ def main():
     def step():
         rl.run(obs, est, ITERATIONS, EPSILON, init=rl.INIT_MEAN, scratch=scratch, stream=stream)
 
+    fp32_peak_tflops(dev)  # the FP32 roofline denominator, measured before the timed region
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize(dev)
@@ -723,7 +767,7 @@ def main():
 
     with_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
     hbm_legs = measure_hbm_legs(dev, stream, cpu=with_cpu)
-    bf16_leg = measure_bf16_leg(dev, stream)
+    bf16_leg = measure_bf16_leg(dev, stream, cpu=with_cpu)
     batch_leg = measure_batch_leg(dev, stream, cpu=with_cpu)
     learned_leg = measure_learned_leg(dev)
     fft_leg = measure_fft_leg(dev, stream)
@@ -738,8 +782,8 @@ def main():
     # roofline of the fused pass (100 launches per step; the two init kernels are tiny,
     # so step time / 100 bounds the average pass duration from above)
     peaks, peak_kind = measured_peaks()
-    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s at the maximum SM clock
+    fp32 = fp32_peak_tflops(dev)
+    fp32_peak = fp32["peak"]
     pass_ms = ms_per_step / (2 * ITERATIONS)
     flops_per_pass = 2.0 * TAPS * VOXELS
     achieved = flops_per_pass / (pass_ms / 1e3) / 1e12
@@ -754,12 +798,14 @@ def main():
         "frac": achieved / fp32_peak,
         "traffic": traffic,
         "kernel": "conv_tile_kernel<15,2,2,TMA> (RL pass A/B)",
-        "peak_source": f"derived: 152 SMs x 128 FP32 FMA/clk x 2 x sm_max_mhz {sm_max:.0f} ({peak_kind} peaks file);"
-                       " no FP32-SIMT peak is measured, the kernel is FP32-pipe bound",
+        "peak_source": (f"measured in this run: FP32 FMA probe (iane_gb_fp32_peak_probe), scalar FFMA "
+                        f"{fp32['scalar_ffma']:.1f} and paired fma.rn.f32x2 {fp32['paired_ffma2']:.1f} TFLOP/s, "
+                        f"the larger taken; nominal {fp32['sms']} SMs x 128 FMA/clk x 2 x max clock = "
+                        f"{fp32['nominal']:.1f}"),
+        "peak_nominal": fp32["nominal"],
         "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": float(peaks.get("hbm_gbs", 6800.0)),
-                "frac": hbm_achieved / float(peaks.get("hbm_gbs", 6800.0)), "alg_bytes_per_pass": alg_bytes_pass},
-        "frac_at_sampled_clock": (achieved / (152 * 256 * clocks["sm_mhz"] * 1e6 / 1e12)
-                                  if clocks.get("sm_mhz") else None),
+                "frac": hbm_achieved / float(peaks.get("hbm_gbs", 6800.0)), "alg_bytes_per_pass": alg_bytes_pass,
+                "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
     }
 
     cpu = None

@@ -262,6 +262,14 @@ def device_status(stream=None) -> None:
     check(lib().iane_gb_device_status(_stream_handle(stream)))
 
 
+def fp32_peak(paired: bool = False, stream=None) -> float:
+    """Measured FP32 FMA throughput of the current device in TFLOP/s: scalar FFMA, or the
+    packed two-lane form (``paired``). Synchronises the stream."""
+    out = ctypes.c_double(0.0)
+    check(lib().iane_gb_fp32_peak_probe(1 if paired else 0, ctypes.byref(out), _stream_handle(stream)))
+    return float(out.value)
+
+
 class RichardsonLucy:
     """Prepared Richardson-Lucy deconvolution for one image shape and PSF.
 

@@ -57,6 +57,8 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_device_status.restype = ctypes.c_int
     l.iane_gb_wait_probe.argtypes = [ctypes.c_uint, vp]
     l.iane_gb_wait_probe.restype = ctypes.c_int
+    l.iane_gb_fp32_peak_probe.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
+    l.iane_gb_fp32_peak_probe.restype = ctypes.c_int
     l.iane_gb_convolve.argtypes = [_VIEW_P, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_uint, vp]
     l.iane_gb_convolve.restype = ctypes.c_int
     l.iane_gb_convolve_separable.argtypes = [_VIEW_P, ctypes.POINTER(_VIEW_P), _VIEW_P, ctypes.c_int, vp]

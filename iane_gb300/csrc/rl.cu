@@ -390,10 +390,10 @@ int rl_run_bf16(iane_gb_rl_plan* plan, const DevView& obs, const DevView& est, i
 // ------------------------------------------------------------------------------------
 // Allocation-free variant (iane_gb_rl_run_noalloc).
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is being captured
-// with a relaxed capture mode that forbids allocation, plugins loaded into a host that owns
-// the device allocator (a pooled allocator or a memory budget the plugin must not bypass),
-// and real-time loops that must not block in the driver's allocator. For them the variant
+// Some callers cannot call cudaMalloc: plugins loaded into a host application that owns the
+// device allocator (a pooled allocator, or a memory budget the plugin must not bypass), and
+// real-time loops that must not block in the driver's allocator, whose cudaMalloc and
+// cudaFree may synchronise the device. For them the variant
 // keeps every byte of RL's scratch -- ratio image, work estimate, sensitivity classes and
 // table, mean partials -- in the file-scope array below, sized for images of at most
 // kNoAllocMaxVoxels padded voxels. Every GPU that loads this library holds the array
@@ -1028,7 +1028,10 @@ int iane_gb_rl_run_noalloc(const iane_gb_view* psf, const iane_gb_view* observed
 		}
 	} else {
 		if (init == IANE_GB_RL_INIT_MEAN) {
-			rl_mean_kernel<<<grid_for(n), 256, 0, st>>>(obs, parts, counter, start, epsilon);
+			// one partial per block in a region of kNoAllocMaxPartials doubles; the kernel's
+			// grid-stride loop covers the image with any grid
+			const int mean_grid = grid_for(n) < kNoAllocMaxPartials ? grid_for(n) : kNoAllocMaxPartials;
+			rl_mean_kernel<<<mean_grid, 256, 0, st>>>(obs, parts, counter, start, epsilon);
 		}
 		rl_init_kernel<<<grid_for(n), 256, 0, st>>>(obs, e_work, pitch, plane, epsilon, init, start);
 	}

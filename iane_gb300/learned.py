@@ -410,12 +410,36 @@ def _rel_l2(a, b) -> float:
     return float((a.double() - b.double()).norm() / b.double().norm())
 
 
+def poisson_deviance(observed, estimate, psf, epsilon: float = 1e-6) -> float:
+    """2 * sum(o log(o / p) - (o - p)) with p = max(estimate (*) psf, eps) (zero border), the
+    negative Poisson log-likelihood up to a constant: the objective every RL iteration lowers."""
+    import torch
+
+    pred = torch.empty_like(estimate)
+    convolve(estimate, psf, pred, "zero")
+    p = pred.double().clamp_min(epsilon)
+    o = observed.double()
+    term = torch.where(o > 0, o * torch.log(o / p), torch.zeros_like(p)) - (o - p)
+    return float(2.0 * term.sum())
+
+
+def data_residual(observed, estimate, psf) -> float:
+    """||estimate (*) psf - observed|| / ||observed|| (zero border)."""
+    pred = estimate.new_empty(estimate.shape)
+    convolve(estimate, psf, pred, "zero")
+    return float((pred.double() - observed.double()).norm() / observed.double().norm())
+
+
 def evaluate(net: WarmStartNet, seed=7, sigma=2.0, peak=1000.0, tolerance=1e-3, reference_iterations=200,
              max_iterations=400, repeats=3, device="cuda", log=None):
     """The 256x256x64 ellipsoid volume (200 ellipsoids, radii 2-20) blurred by the isotropic
     Gaussian PSF of width `sigma`, Poisson counts with peak `peak`. Reference: the
-    `reference_iterations`-iteration FP32 RL result from the flat start. Two stopping rules:
+    `reference_iterations`-iteration FP32 RL result from the flat start. Three stopping rules:
 
+    * "residual": iterate until the data fit is as good as the reference's -- the Poisson
+      deviance of the estimate (RL's own objective) within `tolerance` (relative) of the
+      reference's deviance. Plain RL from the flat start is the judge: a warm start counts
+      when RL from it reaches the residual tolerance that plain RL reaches;
     * "to_reference": iterate until rel-L2(estimate, reference) <= tolerance;
     * "converged": iterate until the relative L2 change of one iteration <= tolerance.
 
@@ -439,23 +463,28 @@ def evaluate(net: WarmStartNet, seed=7, sigma=2.0, peak=1000.0, tolerance=1e-3, 
     reference = torch.empty_like(observed)
     rl32.run(observed, reference, reference_iterations, 1e-6, init=rl32.INIT_MEAN, scratch=s32)
 
+    target_dev = poisson_deviance(observed, reference, psf)
+
     def trajectory(rl, scratch, start):
-        """errors[k] = rel-L2 vs reference after k iterations (k = 0 is the start)."""
+        """errors[k] = rel-L2 vs reference after k iterations (k = 0 is the start); changes[k]
+        = relative change of iteration k; excess[k] = deviance / reference deviance - 1."""
         est = torch.empty_like(observed)
         if start is None:
             est.fill_(float(observed.double().mean().clamp_min(1e-6)))
         else:
             est.copy_(start)
         errors, changes = [_rel_l2(est, reference)], [float("nan")]
+        excess = [poisson_deviance(observed, est, psf) / target_dev - 1.0]
         stats = torch.zeros(2, dtype=torch.float64, device=dev)
         for k in range(max_iterations):
             init = rl.INIT_MEAN if start is None and k == 0 else rl.INIT_GIVEN
             rl.run(observed, est, 1, 1e-6, init=init, scratch=scratch, stats=stats)
             errors.append(_rel_l2(est, reference))
             changes.append(float(stats[1].item()))
-            if errors[-1] <= tolerance and changes[-1] <= tolerance:
+            excess.append(poisson_deviance(observed, est, psf) / target_dev - 1.0)
+            if errors[-1] <= tolerance and changes[-1] <= tolerance and excess[-1] <= tolerance:
                 break
-        return errors, changes, est
+        return errors, changes, excess, est
 
     def first(values, tol):
         for k, v in enumerate(values):
@@ -475,13 +504,15 @@ def evaluate(net: WarmStartNet, seed=7, sigma=2.0, peak=1000.0, tolerance=1e-3, 
             times.append(a.elapsed_time(b))
         return float(np.median(times[1:]))
 
-    e_plain, c_plain, _ = trajectory(rl32, s32, None)
+    e_plain, c_plain, x_plain, _ = trajectory(rl32, s32, None)
     start = net.warm_start(observed, sigma)
     torch.cuda.synchronize()
-    e_learn, c_learn, _ = trajectory(rl16, s16, start)
+    e_learn, c_learn, x_learn, _ = trajectory(rl16, s16, start)
     out = {"volume": [256, 256, 64], "psf": [psf_extent(sigma)] * 3, "sigma": sigma, "peak": peak,
            "tolerance": tolerance, "reference_iterations": reference_iterations,
-           "start_error": {"flat": e_plain[0], "learned": e_learn[0]}}
+           "reference_deviance": target_dev, "reference_data_residual": data_residual(observed, reference, psf),
+           "start_error": {"flat": e_plain[0], "learned": e_learn[0]},
+           "start_deviance_excess": {"flat": x_plain[0], "learned": x_learn[0]}}
     est = torch.empty_like(observed)
 
     def plain(n):
@@ -496,18 +527,22 @@ def evaluate(net: WarmStartNet, seed=7, sigma=2.0, peak=1000.0, tolerance=1e-3, 
 
     net_ms = timed(learned(0))
     out["network_ms"] = net_ms
-    for rule, p_vals, l_vals in (("to_reference", e_plain, e_learn), ("converged", c_plain, c_learn)):
+    for rule, p_vals, l_vals in (("residual", x_plain, x_learn), ("to_reference", e_plain, e_learn),
+                                 ("converged", c_plain, c_learn)):
         n0, n1 = first(p_vals, tolerance), first(l_vals, tolerance)
         r = {"plain_iterations": n0, "learned_iterations": n1}
         if n0 is not None:
             r["plain_ms"] = timed(plain(n0))
             r["plain_error"] = e_plain[n0]
+            r["plain_deviance_excess"] = x_plain[n0]
         if n1 is not None:
             r["learned_ms"] = timed(learned(n1))
             r["learned_error"] = e_learn[n1]
+            r["learned_deviance_excess"] = x_learn[n1]
         else:
-            r["learned_min_error"] = min(e_learn)
-            r["learned_min_error_at"] = int(np.argmin(e_learn))
+            vals = e_learn if rule != "residual" else x_learn
+            r["learned_min"] = min(vals)
+            r["learned_min_at"] = int(np.argmin(vals))
         if n0 is not None and n1 is not None:
             r["speedup"] = r["plain_ms"] / r["learned_ms"]
         out[rule] = r

@@ -108,6 +108,13 @@ int iane_gb_device_status(void* stream);
  * usable. Every device-side wait of this library has the same bound (two seconds). */
 int iane_gb_wait_probe(unsigned int limit_us, void* stream);
 
+/* Diagnostic: measured FP32 fused multiply-add throughput of the current device in TFLOP/s
+ * (2 flops per FMA), the ceiling of FP32-pipe-bound convolutions. paired = 0 issues scalar
+ * FFMA, 1 the packed two-lane fma.rn.f32x2; independent chains on every lane of 8 blocks of
+ * 256 threads per SM, best of three timed launches after a warm-up. Synchronises `stream`.
+ * No counterpart in the reference. */
+int iane_gb_fp32_peak_probe(int paired, double* tflops, void* stream);
+
 /*
  * Direct N-D convolution. Replaces iane::convolve for CUDA memory views
  * (reference include/iane/algorithms/convolution.hpp:97-117, with the extent check of
@@ -353,10 +360,10 @@ int iane_gb_cnn_adam(float* params, uint16_t* params16, const float* grads, floa
 /*
  * Allocation-free Richardson-Lucy. No counterpart in the reference.
  *
- * For callers that must not allocate device memory: code recorded into a CUDA graph under
- * a capture mode that forbids allocation, plugins inside a host application that owns the
- * device allocator or enforces a memory budget, and latency-bound loops that cannot block
- * in the allocator. It runs the same iteration as iane_gb_rl_prepare + iane_gb_rl_run, with
+ * For callers that must not allocate device memory: plugins inside a host application that
+ * owns the device allocator or enforces a memory budget, and latency-bound loops that cannot
+ * block in the allocator (cudaMalloc and cudaFree may synchronise the whole device). It runs
+ * the same iteration as iane_gb_rl_prepare + iane_gb_rl_run, with
  * the same kernels and results, but calls no cudaMalloc, cudaFree or other allocating
  * routine: its scratch (ratio image, work estimate, edge-sensitivity table, reduction
  * partials) is one static device array of about 32.4 MiB that every GPU loading this
@@ -367,7 +374,8 @@ int iane_gb_cnn_adam(float* params, uint16_t* params16, const float* grads, floa
  * <= 31, height and depth <= 63, at most 32768 taps. No statistics are produced.
  *
  * The first call on a device looks up the array's device address with that device
- * current; make that first call before any stream capture. All calls share the one array:
+ * current; make that first call before any stream capture. The mean start's reduction uses
+ * at most 4096 blocks of partial sums. All calls share the one array:
  * calls whose GPU work overlaps (different streams, or different host threads, without
  * ordering between them) race on it and corrupt each other's results.
  */

@@ -64,6 +64,12 @@ def oracle_lib():
         lib.oracle_sensitivity.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p, ctypes.c_int]
         lib.oracle_sensitivity.restype = ctypes.c_int
+        lib.oracle_det_rl_volume.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_int]
+        lib.oracle_det_rl_volume.restype = ctypes.c_int
         _oracle = lib
     return _oracle
 
@@ -183,6 +189,24 @@ def sensitivity(psf_adjoint: np.ndarray, shape, threads: int | None = None) -> n
     _check(oracle_lib().oracle_sensitivity(k.ctypes.data, _extent(k.shape), k.ndim, _extent(shape),
                                            out.ctypes.data, threads), "sensitivity")
     return out
+
+
+def det_rl_volume(extent_xyz, count: int, psf: np.ndarray, seed: int, radius=(2.0, 20.0),
+                  intensity=(50.0, 1000.0), background: float = 10.0, threads: int | None = None):
+    """Deterministic ellipsoid phantom, its zero-border blur by ``psf`` and Poisson counts
+    (``det_synth.c``): the same bits on every platform. Returns (observed, truth), float32
+    C-ordered arrays of shape (nz, ny, nx)."""
+    threads = default_threads() if threads is None else threads
+    nx, ny, nz = (int(v) for v in extent_xyz)
+    k = np.ascontiguousarray(psf, dtype=np.float32)
+    assert k.ndim == 3
+    truth = np.zeros((nz, ny, nx), np.float32)
+    observed = np.zeros((nz, ny, nx), np.float32)
+    status = oracle_lib().oracle_det_rl_volume(nx, ny, nz, count, radius[0], radius[1], intensity[0], intensity[1],
+                                               background, seed, k.ctypes.data, _extent(k.shape),
+                                               truth.ctypes.data, observed.ctypes.data, threads)
+    _check(status, "det_rl_volume")
+    return observed, truth
 
 
 def to_gray8(values: np.ndarray) -> np.ndarray:

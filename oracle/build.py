@@ -1,7 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-* ``oracle/liboracle.so`` -- the C restatement in ``iane_oracle.c`` (gcc, pthreads).
-  Built everywhere, including the GPU host.
+* ``oracle/liboracle.so`` -- the C restatement in ``iane_oracle.c`` (gcc, pthreads) and the
+  deterministic input generator in ``det_synth.c``. Built everywhere, including the GPU host.
 * ``oracle/_ref/libiane_ref.so`` -- ``ref_shim.cpp`` compiled against the reference's own
   headers, read in place from the reference checkout (``IANE_REFERENCE`` or
   ``/root/reference``). Built only where that checkout exists; never copied.
@@ -34,13 +34,13 @@ def _stale(target: Path, sources: list[Path]) -> bool:
 
 
 def build_oracle(force: bool = False) -> Path:
-    src = HERE / "iane_oracle.c"
+    sources = [HERE / "iane_oracle.c", HERE / "det_synth.c"]
     header = HERE.parent / "include" / "iane_gb" / "capi.h"
-    if force or _stale(ORACLE_LIB, [src, header]):
+    if force or _stale(ORACLE_LIB, sources + [header]):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
         subprocess.check_call([
             "gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
-            str(src), "-o", str(tmp), "-lm",
+            *[str(s) for s in sources], "-o", str(tmp), "-lm",
         ])
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB

@@ -6,7 +6,7 @@
  * product path. It restates, in plain C, the reference algorithm so that the GPU
  * kernels can be compared with it on the GPU host, where the reference sources are
  * not available. It is pinned against the reference itself (the reference's headers
- * compiled here by oracle/build.py into oracle/_ref, see tests/test_oracle_vs_ref.py)
+ * compiled here by oracle/build.py into oracle/_ref, see tests/test_oracle.py)
  * and against the golden vectors in tests/golden/.
  *
  * Reference (JanKolomaznik/iane) citations:

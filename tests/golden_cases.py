@@ -66,3 +66,15 @@ def bench_pattern(width, height):
 
 def bench_sha256() -> str:
     return str(data()["bench_u8_2560x1920__sha256"])
+
+
+CONFIGS = Path(__file__).resolve().parent / "golden" / "configs.npz"
+_configs = None
+
+
+def configs():
+    """The benchmark configurations run by the reference (tests/golden/make_config_fixtures.py)."""
+    global _configs
+    if _configs is None:
+        _configs = dict(np.load(CONFIGS))
+    return _configs
