@@ -405,7 +405,8 @@ def measure_bf16_leg(dev, stream, reps=5, cpu=True):
 def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     """Batched uneven 2-D RL: 256 images, sides log-uniform in [64, 1024], own Gaussian PSF
     each (odd size 3-31, sigma 0.5-5), Poisson noise, 30 iterations, one CUDA-graph replay
-    per run of persistent work-queue passes, autotuned tile shapes."""
+    per run holding ONE persistent launch over the work queue of every pass of every image,
+    autotuned CTAs per SM and queue order."""
     import numpy as np
     import torch
 
@@ -439,7 +440,7 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     ms = a.elapsed_time(b) / reps
     pixels = sum(o.numel() for o in obs)
     macs = sum(o.numel() * p.size for o, p in zip(obs, psfs)) * 2 * iterations
-    widths = batch.tile_widths()
+    bps, order = batch.launch_config()
     batch.close()
     assert all(bool(torch.isfinite(o).all()) for o in outs)
     peaks, _ = measured_peaks()
@@ -449,7 +450,8 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     res = {"images": len(obs), "pixels": pixels, "iterations": iterations, "ms_per_run": ms,
            "gvoxel_s": 2 * iterations * pixels / (ms / 1e3) / 1e9, "tflops_useful": 2 * macs / (ms / 1e3) / 1e12,
            "gbs_algorithmic": alg_bytes / (ms / 1e3) / 1e9,
-           "tiles_64": int(sum(1 for w in widths if w == 64)), "tiles_32": int(sum(1 for w in widths if w == 32)),
+           "launch": {"persistent_launches_per_run": 1, "ctas_per_sm": bps,
+                      "queue_order": ["largest images first", "by PSF width"][order], "tile": "64x64"},
            "prepare_s": prepare_s}
     res["frac_of_fp32_peak"] = res["tflops_useful"] / fp32
     res["frac_of_hbm_peak"] = res["gbs_algorithmic"] / hbm

@@ -357,10 +357,12 @@ class RichardsonLucy:
 class RichardsonLucyBatch:
     """Richardson-Lucy over many 2-D images of uneven size, each with its own PSF.
 
-    One persistent launch per pass and tile shape over a device work queue; the schedule of
-    a run is captured into a CUDA graph and replayed while the tensors and parameters stay
-    the same. ``autotune=True`` times 32x32 against 64x64 tiles per (shape, PSF size) and
-    caches the choice (file named by ``IANE_GB_TUNE_CACHE``)."""
+    The whole run -- every pass of every iteration of every image -- is one persistent launch
+    over a device work queue of 64x64 tiles, each image's pass waiting only for that image's
+    previous pass; the run (counter reset, start values, the launch) is captured into a CUDA
+    graph and replayed while the tensors and parameters stay the same. ``autotune=True`` times
+    the launch's CTAs per SM and queue order on this batch and caches the choice per batch
+    signature (file named by ``IANE_GB_TUNE_CACHE``)."""
 
     def __init__(self, psfs, shapes, autotune: bool = False, stream=None):
         self.shapes = [tuple(int(v) for v in s) for s in shapes]
@@ -379,6 +381,13 @@ class RichardsonLucyBatch:
         out = (ctypes.c_int32 * len(self.shapes))()
         check(lib().iane_gb_rl_batch_tiles(self._batch, out))
         return list(out)
+
+    def launch_config(self):
+        """(CTAs per SM, queue order) of the persistent launch: 0 = largest images first,
+        1 = grouped by PSF width."""
+        bps, order = ctypes.c_int32(0), ctypes.c_int32(0)
+        check(lib().iane_gb_rl_batch_config(self._batch, ctypes.byref(bps), ctypes.byref(order)))
+        return int(bps.value), int(order.value)
 
     def run(self, observed, estimates, iterations: int, epsilon: float = 1e-6, init: int = abi.RL_INIT_OBSERVED,
             scratch=None, stream=None):

@@ -1,5 +1,6 @@
-// Batched Richardson-Lucy: plans, autotuned tile shapes, the CUDA-graph schedule and the
-// C-ABI entry points iane_gb_rl_batch_*. See rl_batch.cuh for the execution design.
+// Batched Richardson-Lucy: plans, the work queue, the autotuned launch configuration, the
+// CUDA graph of a run and the C-ABI entry points iane_gb_rl_batch_*. See rl_batch.cuh for the
+// execution design.
 #include "kernels.h"
 #include "rl_batch.cuh"
 
@@ -86,8 +87,6 @@ __global__ void batch_init_kernel(const InitDesc* d, const float* starts, float 
 	}
 }
 
-int occupancy_grid(int wx, bool wide, size_t smem, size_t items);
-
 bool work_layout(const DevView& v, long long pitch)
 {
 	if (v.dtype != IANE_GB_F32 || v.stride[0] != 4 || reinterpret_cast<uintptr_t>(v.ptr) % 16 != 0) return false;
@@ -95,13 +94,39 @@ bool work_layout(const DevView& v, long long pitch)
 	return true;
 }
 
+int tiles_of(int n) { return (n + kBatchTile - 1) / kBatchTile; }
+
+// Queue orders of one phase's items (the autotuner picks one per batch).
+constexpr int kOrderLargestFirst = 0; // images by descending tile count
+constexpr int kOrderByWidth = 1;      // images by PSF width, then by descending tile count
+constexpr int kOrders = 2;
+
+std::vector<BatchItem> make_items(const std::vector<int>& nx, const std::vector<int>& ny, const std::vector<int>& kx,
+	int order)
+{
+	const int n = static_cast<int>(nx.size());
+	std::vector<int> idx(n);
+	for (int i = 0; i < n; ++i) idx[i] = i;
+	auto tiles = [&](int i) { return tiles_of(nx[i]) * tiles_of(ny[i]); };
+	std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+		if (order == kOrderByWidth && kx[a] != kx[b]) return kx[a] < kx[b];
+		return tiles(a) > tiles(b);
+	});
+	std::vector<BatchItem> items;
+	for (int i : idx) {
+		for (int t = 0; t < tiles(i); ++t) items.push_back(BatchItem{i, t});
+	}
+	return items;
+}
+
 // ---------------------------------------------------------------------------------------
-// autotuner: tile shape per (shape, PSF size, dtype, SM count), cached in a text file
+// autotuner: CTAs per SM and queue order per batch (shapes, PSF sizes, dtype, SM count),
+// cached in a text file
 
 struct TuneCache {
 	std::mutex lock;
 	bool loaded = false;
-	std::map<std::string, int> choice;
+	std::map<std::string, std::pair<int, int>> choice; // key -> (CTAs per SM, order)
 	std::string path;
 };
 
@@ -118,10 +143,26 @@ std::string cache_path()
 	return "iane_gb300_tune.txt";
 }
 
-std::string tune_key(int nx, int ny, int kx, int ky)
+// The batch signature: image count, a 64-bit FNV-1a hash of every (nx, ny, kx, ky), dtype, SMs.
+std::string tune_key(const std::vector<int>& nx, const std::vector<int>& ny, const std::vector<int>& kx,
+	const std::vector<int>& ky)
 {
+	uint64_t h = 1469598103934665603ull;
+	auto mix = [&](int v) {
+		for (int b = 0; b < 4; ++b) {
+			h ^= static_cast<uint64_t>((static_cast<uint32_t>(v) >> (8 * b)) & 0xffu);
+			h *= 1099511628211ull;
+		}
+	};
+	for (size_t i = 0; i < nx.size(); ++i) {
+		mix(nx[i]);
+		mix(ny[i]);
+		mix(kx[i]);
+		mix(ky[i]);
+	}
 	std::ostringstream k;
-	k << "rl2d-classes f32 " << nx << "x" << ny << " psf " << kx << "x" << ky << " sms " << device_sm_count();
+	k << "rl2d-batch f32 images " << nx.size() << " shapes " << std::hex << h << std::dec << " sms "
+	  << device_sm_count();
 	return k.str();
 }
 
@@ -133,142 +174,37 @@ void load_cache(TuneCache& c)
 	std::ifstream in(c.path);
 	std::string line;
 	while (std::getline(in, line)) {
-		// "<key> | <ms 32x32> <ms 64x64> |<choice>"
+		// "<key> | <ms per configuration ...> | <CTAs per SM> <order>"
 		const auto first = line.find(" | ");
-		const auto last = line.rfind('|');
-		if (first == std::string::npos || last == std::string::npos || last <= first + 1) continue;
-		const int wx = std::atoi(line.c_str() + last + 1);
-		if (wx == 1 || wx == 2) c.choice[line.substr(0, first)] = wx;
+		const auto last = line.rfind(" | ");
+		if (first == std::string::npos || last == first) continue;
+		std::istringstream tail(line.substr(last + 3));
+		int bps = 0, order = -1;
+		if (tail >> bps >> order && bps > 0 && order >= 0 && order < kOrders) {
+			c.choice[line.substr(0, first)] = {bps, order};
+		}
 	}
 }
 
 }  // namespace
-
-int batch_autotune(const std::vector<int>& nx, const std::vector<int>& ny, const std::vector<int>& kx,
-	const std::vector<int>& ky, const std::vector<iane_gb_rl_plan*>& plans, std::vector<int>& wx, cudaStream_t stream)
-{
-	TuneCache& cache = tune_cache();
-	std::lock_guard<std::mutex> guard(cache.lock);
-	load_cache(cache);
-	int* status = device_status_ptr();
-	if (!status) return IANE_GB_CUDA_ERROR;
-	const int n = static_cast<int>(nx.size());
-	std::vector<int> todo;
-	for (int i = 0; i < n; ++i) {
-		const auto it = cache.choice.find(tune_key(nx[i], ny[i], kx[i], ky[i]));
-		if (it != cache.choice.end()) {
-			wx[i] = it->second;
-		} else {
-			todo.push_back(i);
-		}
-	}
-	if (todo.empty()) return IANE_GB_OK;
-	const int sms = device_sm_count();
-	size_t max_bytes = 0;
-	for (int i : todo) {
-		max_bytes = std::max(max_bytes, align_up(static_cast<size_t>((nx[i] + 3) & ~3) * ny[i] * 4));
-	}
-	const int max_copies = 256;
-	char* buf = nullptr;
-	BatchImage* d_images = nullptr;
-	BatchItem* d_items = nullptr;
-	unsigned int* counter = nullptr;
-	const size_t max_items = 1 << 16;
-	cudaEvent_t t0 = nullptr, t1 = nullptr;
-	auto release = [&](int code) {
-		cudaFree(buf);
-		cudaFree(d_images);
-		cudaFree(d_items);
-		cudaFree(counter);
-		if (t0) cudaEventDestroy(t0);
-		if (t1) cudaEventDestroy(t1);
-		return code;
-	};
-	if (cudaMalloc(&buf, 3 * max_bytes) != cudaSuccess || cudaMemsetAsync(buf, 0, 3 * max_bytes, stream) != cudaSuccess ||
-	    cudaMalloc(&d_images, max_copies * sizeof(BatchImage)) != cudaSuccess ||
-	    cudaMalloc(&d_items, max_items * sizeof(BatchItem)) != cudaSuccess ||
-	    cudaMalloc(&counter, 8 * sizeof(unsigned int)) != cudaSuccess || cudaEventCreate(&t0) != cudaSuccess ||
-	    cudaEventCreate(&t1) != cudaSuccess) {
-		return release(cuda_fail(cudaGetLastError(), "autotune: allocate"));
-	}
-	std::ofstream log(cache.path, std::ios::app);
-	for (int i : todo) {
-		const std::string key = tune_key(nx[i], ny[i], kx[i], ky[i]);
-		if (cache.choice.count(key)) {
-			wx[i] = cache.choice[key];
-			continue;
-		}
-		const long long pitch = (static_cast<long long>(nx[i]) + 3) & ~3LL, plane = pitch * ny[i];
-		float ms[2] = {0.0f, 0.0f};
-		for (int w = 1; w <= 2; ++w) {
-			const int t = 32 * w;
-			const int tiles = ((nx[i] + t - 1) / t) * ((ny[i] + t - 1) / t);
-			// enough copies of this image's tiles to occupy every SM several times over
-			const int copies = std::min(max_copies, std::max(1, (8 * sms + tiles - 1) / tiles));
-			std::vector<BatchImage> host(copies);
-			BatchImage im{};
-			int st = encode_tensor_map_f32(&im.map_est, buf, nx[i], ny[i], 1, pitch * 4, plane * 4, tile_pitch(kx[i], w),
-				t + 2 * (ky[i] / 2));
-			if (st) return release(st);
-			im.map_ratio = im.map_est;
-			rl_plan_fill_passes(plans[i], &im.pass_a, &im.pass_b, &im.epi_a, &im.epi_b, status);
-			im.epi_a.ratio = reinterpret_cast<float*>(buf + max_bytes);
-			im.epi_a.obs = buf + 2 * max_bytes;
-			im.epi_a.os[0] = 4;
-			im.epi_a.os[1] = pitch * 4;
-			im.epi_a.eps = 1e-6f;
-			im.kx = kx[i];
-			im.tiles_x = (nx[i] + t - 1) / t;
-			for (auto& h : host) h = im;
-			std::vector<BatchItem> items;
-			for (int c = 0; c < copies && static_cast<size_t>(items.size()) + tiles <= max_items; ++c)
-				for (int k = 0; k < tiles; ++k) items.push_back(BatchItem{c, k});
-			if (cudaMemcpy(d_images, host.data(), copies * sizeof(BatchImage), cudaMemcpyHostToDevice) != cudaSuccess ||
-			    cudaMemcpy(d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) != cudaSuccess) {
-				return release(cuda_fail(cudaGetLastError(), "autotune: upload"));
-			}
-			const size_t smem = batch_tile_smem(w, kx[i], ky[i]);
-			const int grid = occupancy_grid(w, batch_wide(kx[i]), smem, items.size());
-			for (int rep = 0; rep < 4; ++rep) {
-				if (rep == 1) cudaEventRecord(t0, stream);
-				cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream);
-				st = launch_batch_pass(w, batch_wide(kx[i]), false, d_images, d_items, static_cast<int>(items.size()), counter, 0, grid, smem,
-					stream);
-				if (st) return release(st);
-			}
-			cudaEventRecord(t1, stream);
-			IANE_GB_CUDA(cudaEventSynchronize(t1), "autotune: time");
-			float elapsed = 0.0f;
-			cudaEventElapsedTime(&elapsed, t0, t1);
-			ms[w - 1] = elapsed / (3.0f * static_cast<float>(items.size() / tiles));
-		}
-		wx[i] = ms[0] < ms[1] ? 1 : 2;
-		cache.choice[key] = wx[i];
-		if (log) log << key << " | " << ms[0] << " " << ms[1] << " |" << wx[i] << "\n";
-	}
-	return release(IANE_GB_OK);
-}
-
 }  // namespace iane_gb
 
 struct iane_gb_rl_batch {
 	int count = 0;
 	std::vector<iane_gb_rl_plan*> plans;
-	std::vector<int> nx, ny, kx, ky, wx;
+	std::vector<int> nx, ny, kx, ky;
 	std::vector<long long> pitch;
 	std::vector<size_t> off;               // per image: ratio at off, work at off + image bytes
 	std::vector<size_t> img_bytes;
-	// per group (batch_group: 32x32 / 64x64 tiles x narrow / wide PSFs)
-	std::vector<iane_gb::BatchItem> items[iane_gb::kBatchGroups];
-	iane_gb::BatchItem* d_items[iane_gb::kBatchGroups] = {};
-	size_t smem[iane_gb::kBatchGroups] = {};
-	int grid[iane_gb::kBatchGroups] = {};
+	std::vector<iane_gb::BatchItem> items; // one phase of the queue
+	iane_gb::BatchItem* d_items = nullptr;
+	size_t smem = 0;                       // dynamic shared memory of the launch
+	int blocks_per_sm = 1;                 // resident CTAs per SM the launch uses
+	int order = 0;                         // queue order (autotuned)
 	iane_gb::BatchImage* d_images = nullptr;
 	iane_gb::InitDesc* d_init = nullptr;
-	size_t parts_off = 0, counter_off = 0, scratch_bytes = 0;
-	cudaStream_t side[iane_gb::kBatchGroups] = {};  // side[0] carries the capture
-	cudaEvent_t fork = nullptr;
-	cudaEvent_t join[iane_gb::kBatchGroups] = {};
+	size_t parts_off = 0, sync_off = 0, scratch_bytes = 0;
+	cudaStream_t capture = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	std::string key;
 };
@@ -276,31 +212,29 @@ struct iane_gb_rl_batch {
 namespace iane_gb {
 namespace {
 
-// Build descriptors for one run and the graph that performs it.
-int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int iterations, float eps, int init,
-	char* base)
+// Device descriptors of every image for a run over `base` (the scratch).
+int fill_images(const iane_gb_rl_batch* b, const DevView* obs, const DevView* est, float eps, char* base,
+	std::vector<BatchImage>& host, std::vector<InitDesc>& idesc)
 {
 	const int n = b->count;
-	std::vector<BatchImage> host(n);
-	std::vector<InitDesc> idesc(n);
+	host.assign(n, BatchImage{});
+	idesc.assign(n, InitDesc{});
 	int* status = device_status_ptr();
 	if (!status) return IANE_GB_CUDA_ERROR;
 	for (int i = 0; i < n; ++i) {
-		const iane_gb_rl_plan* p = b->plans[i];
-		(void)p;
-		const int nx = b->nx[i], ny = b->ny[i], kxi = b->kx[i], kyi = b->ky[i], w = b->wx[i];
+		const int nx = b->nx[i], ny = b->ny[i], kxi = b->kx[i], kyi = b->ky[i];
 		const long long pitch = b->pitch[i], plane = pitch * ny;
 		float* ratio = reinterpret_cast<float*>(base + b->off[i]);
 		float* work = reinterpret_cast<float*>(base + b->off[i] + b->img_bytes[i]);
-		const bool in_place = work_layout(est[i], pitch);
+		const bool in_place = est && work_layout(est[i], pitch);
 		float* e_work = in_place ? reinterpret_cast<float*>(est[i].ptr) : work;
 		BatchImage& im = host[i];
 		std::memset(&im, 0, sizeof im);
-		int st = encode_tensor_map_f32(&im.map_est, e_work, nx, ny, 1, pitch * 4, plane * 4, tile_pitch(kxi, w),
-			32 * w + 2 * (kyi / 2));
+		int st = encode_tensor_map_f32(&im.map_est, e_work, nx, ny, 1, pitch * 4, plane * 4, tile_pitch(kxi, 2),
+			kBatchTile + 2 * (kyi / 2));
 		if (st) return st;
-		st = encode_tensor_map_f32(&im.map_ratio, ratio, nx, ny, 1, pitch * 4, plane * 4, tile_pitch(kxi, w),
-			32 * w + 2 * (kyi / 2));
+		st = encode_tensor_map_f32(&im.map_ratio, ratio, nx, ny, 1, pitch * 4, plane * 4, tile_pitch(kxi, 2),
+			kBatchTile + 2 * (kyi / 2));
 		if (st) return st;
 		rl_plan_fill_passes(b->plans[i], &im.pass_a, &im.pass_b, &im.epi_a, &im.epi_b, status);
 		im.epi_a.ratio = ratio;
@@ -310,27 +244,52 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 		im.epi_a.eps = eps;
 		im.epi_b.est = e_work;
 		im.epi_b.eps = eps;
-		im.epi_b.out = est[i].ptr;
-		for (int a = 0; a < 3; ++a) im.epi_b.outs[a] = est[i].stride[a];
-		im.epi_b.out_u8 = est[i].dtype == IANE_GB_U8;
+		if (est) {
+			im.epi_b.out = est[i].ptr;
+			for (int a = 0; a < 3; ++a) im.epi_b.outs[a] = est[i].stride[a];
+			im.epi_b.out_u8 = est[i].dtype == IANE_GB_U8;
+		}
 		im.kx = kxi;
-		im.tiles_x = (nx + 32 * w - 1) / (32 * w);
-		im.write_out_final = in_place ? 0 : 1;
+		im.tiles_x = tiles_of(nx);
+		im.tiles = tiles_of(nx) * tiles_of(ny);
+		im.write_out_final = in_place || !est ? 0 : 1;
 		idesc[i].obs = obs[i];
-		idesc[i].est = est[i];
+		if (est) idesc[i].est = est[i];
 		idesc[i].work = e_work;
 		idesc[i].pitch = pitch;
 		idesc[i].in_place = in_place ? 1 : 0;
 	}
+	return IANE_GB_OK;
+}
+
+BatchSync sync_words(const iane_gb_rl_batch* b, char* base)
+{
+	unsigned int* words = reinterpret_cast<unsigned int*>(base + b->sync_off);
+	return BatchSync{words, reinterpret_cast<int*>(words + 1), words + 2};
+}
+
+size_t sync_bytes(int count) { return static_cast<size_t>(count + 2) * sizeof(unsigned int); }
+
+// Build descriptors for one run and the graph that performs it: clear the queue, abort flag
+// and completion counters, the start values, then the one persistent launch.
+int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int iterations, float eps, int init,
+	char* base)
+{
+	const int n = b->count;
+	std::vector<BatchImage> host;
+	std::vector<InitDesc> idesc;
+	int st = fill_images(b, obs, est, eps, base, host, idesc);
+	if (st) return st;
 	IANE_GB_CUDA(cudaMemcpy(b->d_images, host.data(), n * sizeof(BatchImage), cudaMemcpyHostToDevice),
 		"batch: upload image descriptors");
 	IANE_GB_CUDA(cudaMemcpy(b->d_init, idesc.data(), n * sizeof(InitDesc), cudaMemcpyHostToDevice),
 		"batch: upload start descriptors");
+	int* status = device_status_ptr();
+	if (!status) return IANE_GB_CUDA_ERROR;
 
-	double* parts = reinterpret_cast<double*>(base + b->parts_off);
-	float* starts = reinterpret_cast<float*>(parts);
-	unsigned int* counters = reinterpret_cast<unsigned int*>(base + b->counter_off);
-	cudaStream_t s0 = b->side[0];
+	float* starts = reinterpret_cast<float*>(base + b->parts_off);
+	const BatchSync sync = sync_words(b, base);
+	cudaStream_t s0 = b->capture;
 	cudaGraph_t graph = nullptr;
 	IANE_GB_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal), "batch: begin capture");
 	auto abort_capture = [&](int code) {
@@ -339,44 +298,22 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 		if (g) cudaGraphDestroy(g);
 		return code;
 	};
-	if (cudaMemsetAsync(counters, 0, static_cast<size_t>(2 * kBatchGroups * (iterations + 1)) * sizeof(unsigned int),
-	        s0) != cudaSuccess) {
-		return abort_capture(cuda_fail(cudaGetLastError(), "batch: clear counters"));
+	if (cudaMemsetAsync(sync.queue, 0, sync_bytes(n), s0) != cudaSuccess) {
+		return abort_capture(cuda_fail(cudaGetLastError(), "batch: clear queue"));
 	}
 	if (init == IANE_GB_RL_INIT_MEAN) {
 		batch_mean_kernel<<<n, 256, 0, s0>>>(b->d_init, starts, eps);
 	}
 	batch_init_kernel<<<dim3(n, 16), 256, 0, s0>>>(b->d_init, starts, eps, init);
-	for (int t = 0; t < iterations; ++t) {
-		for (int pass = 0; pass < 2; ++pass) {
-			unsigned int* c = counters + 2 * kBatchGroups * t + kBatchGroups * pass;
-			if (cudaEventRecord(b->fork, s0) != cudaSuccess) {
-				return abort_capture(cuda_fail(cudaGetLastError(), "batch: fork"));
-			}
-			for (int g = 1; g < kBatchGroups; ++g) {
-				if (!b->items[g].empty() && cudaStreamWaitEvent(b->side[g], b->fork, 0) != cudaSuccess) {
-					return abort_capture(cuda_fail(cudaGetLastError(), "batch: fork"));
-				}
-			}
-			// the larger groups first on the capture stream; every group on its own branch
-			for (int g = 0; g < kBatchGroups; ++g) {
-				if (b->items[g].empty()) continue;
-				const int st = launch_batch_pass(1 + (g & 1), (g & 2) != 0, pass == 1, b->d_images, b->d_items[g],
-					static_cast<int>(b->items[g].size()), c + g, t == iterations - 1, b->grid[g], b->smem[g],
-					g == 0 ? s0 : b->side[g]);
-				if (st) return abort_capture(st);
-			}
-			for (int g = 1; g < kBatchGroups; ++g) {
-				if (b->items[g].empty()) continue;
-				if (cudaEventRecord(b->join[g], b->side[g]) != cudaSuccess ||
-				    cudaStreamWaitEvent(s0, b->join[g], 0) != cudaSuccess) {
-					return abort_capture(cuda_fail(cudaGetLastError(), "batch: join"));
-				}
-			}
-		}
-	}
-	if (iterations == 0) {
+	if (iterations > 0) {
+		st = launch_batch_persistent(b->d_images, b->d_items, static_cast<int>(b->items.size()), 2 * iterations, sync,
+			status, b->blocks_per_sm * device_sm_count(), b->smem, s0);
+		if (st) return abort_capture(st);
+	} else {
 		batch_init_kernel<<<dim3(n, 16), 256, 0, s0>>>(b->d_init, starts, eps, -1);
+	}
+	if (cudaGetLastError() != cudaSuccess) {
+		return abort_capture(cuda_fail(cudaGetLastError(), "batch: capture launches"));
 	}
 	IANE_GB_CUDA(cudaStreamEndCapture(s0, &graph), "batch: end capture");
 	if (b->exec) {
@@ -389,31 +326,114 @@ int build_graph(iane_gb_rl_batch* b, const DevView* obs, const DevView* est, int
 	return IANE_GB_OK;
 }
 
-int occupancy_grid(int wx, bool wide, size_t smem, size_t items)
+// Choose CTAs per SM (1 .. occupancy) and the queue order by timing a two-iteration run of the
+// whole batch per candidate on scratch images (observed = 1), once per batch signature.
+int autotune(iane_gb_rl_batch* b, cudaStream_t stream)
 {
-	int per_sm = 1;
-	const size_t total = smem + 32;
-	const void* kernel = batch_kernel_handle(wx, wide);
-	cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(total));
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * wx * wx, total);
-	const long long g = static_cast<long long>(device_sm_count()) * std::max(1, per_sm);
-	return static_cast<int>(std::max<long long>(1, std::min<long long>(g, static_cast<long long>(items))));
-}
-
-void fill_items(iane_gb_rl_batch* b)
-{
-	for (int g = 0; g < kBatchGroups; ++g) b->items[g].clear();
-	std::vector<int> order(b->count);
-	for (int i = 0; i < b->count; ++i) order[i] = i;
-	// group images by PSF width so that consecutive work items run the same kernel code
-	std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->kx[a] < b->kx[c]; });
-	for (int i : order) {
-		const int w = b->wx[i], t = 32 * w;
-		const int tiles = ((b->nx[i] + t - 1) / t) * ((b->ny[i] + t - 1) / t);
-		const int g = batch_group(w, b->kx[i]);
-		for (int k = 0; k < tiles; ++k) b->items[g].push_back(BatchItem{i, k});
-		b->smem[g] = std::max(b->smem[g], batch_tile_smem(w, b->kx[i], b->ky[i]));
+	TuneCache& cache = tune_cache();
+	std::lock_guard<std::mutex> guard(cache.lock);
+	load_cache(cache);
+	const std::string key = tune_key(b->nx, b->ny, b->kx, b->ky);
+	const auto hit = cache.choice.find(key);
+	const int max_bps = batch_blocks_per_sm(b->smem);
+	if (hit != cache.choice.end()) {
+		b->blocks_per_sm = std::min(hit->second.first, max_bps);
+		b->order = hit->second.second;
+		return IANE_GB_OK;
 	}
+	int* status = device_status_ptr();
+	if (!status) return IANE_GB_CUDA_ERROR;
+	const int n = b->count;
+	size_t obs_bytes = 0;
+	std::vector<size_t> obs_off(n);
+	for (int i = 0; i < n; ++i) {
+		obs_off[i] = obs_bytes;
+		obs_bytes += (static_cast<size_t>(b->pitch[i]) * b->ny[i] * 4 + 255) & ~size_t(255);
+	}
+	char* buf = nullptr;
+	BatchImage* d_images = nullptr;
+	BatchItem* d_items = nullptr;
+	cudaEvent_t t0 = nullptr, t1 = nullptr;
+	auto release = [&](int code) {
+		cudaFree(buf);
+		cudaFree(d_images);
+		cudaFree(d_items);
+		if (t0) cudaEventDestroy(t0);
+		if (t1) cudaEventDestroy(t1);
+		return code;
+	};
+	const size_t run_bytes = b->scratch_bytes;
+	if (cudaMalloc(&buf, run_bytes + obs_bytes) != cudaSuccess || cudaMalloc(&d_images, n * sizeof(BatchImage)) != cudaSuccess ||
+	    cudaMalloc(&d_items, b->items.size() * sizeof(BatchItem)) != cudaSuccess || cudaEventCreate(&t0) != cudaSuccess ||
+	    cudaEventCreate(&t1) != cudaSuccess) {
+		return release(cuda_fail(cudaGetLastError(), "autotune: allocate"));
+	}
+	char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(buf) + kAlignB - 1) / kAlignB * kAlignB);
+	char* obs_base = buf + run_bytes;
+	std::vector<float> ones;
+	std::vector<DevView> obs(n);
+	for (int i = 0; i < n; ++i) {
+		DevView& v = obs[i];
+		v = DevView{};
+		v.ptr = obs_base + obs_off[i];
+		v.dtype = IANE_GB_F32;
+		v.rank = 2;
+		v.ext[0] = b->nx[i];
+		v.ext[1] = b->ny[i];
+		v.ext[2] = 1;
+		v.stride[0] = 4;
+		v.stride[1] = b->pitch[i] * 4;
+		v.stride[2] = v.stride[1] * b->ny[i];
+		ones.assign(static_cast<size_t>(b->pitch[i]) * b->ny[i], 1.0f);
+		if (cudaMemcpy(v.ptr, ones.data(), ones.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+			return release(cuda_fail(cudaGetLastError(), "autotune: observed"));
+		}
+	}
+	std::vector<BatchImage> host;
+	std::vector<InitDesc> idesc;
+	int st = fill_images(b, obs.data(), nullptr, 1e-6f, base, host, idesc);
+	if (st) return release(st);
+	IANE_GB_CUDA(cudaMemset(base, 0, b->parts_off), "autotune: clear images");
+	if (cudaMemcpy(d_images, host.data(), n * sizeof(BatchImage), cudaMemcpyHostToDevice) != cudaSuccess) {
+		return release(cuda_fail(cudaGetLastError(), "autotune: upload"));
+	}
+	const BatchSync sync = sync_words(b, base);
+	const int T = static_cast<int>(b->items.size());
+	const int sms = device_sm_count();
+	std::ostringstream timings;
+	float best = 0.0f;
+	for (int order = 0; order < kOrders; ++order) {
+		const std::vector<BatchItem> items = make_items(b->nx, b->ny, b->kx, order);
+		if (cudaMemcpy(d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) != cudaSuccess) {
+			return release(cuda_fail(cudaGetLastError(), "autotune: upload items"));
+		}
+		for (int bps = 1; bps <= max_bps; ++bps) {
+			float ms = 0.0f;
+			for (int rep = 0; rep < 3; ++rep) {
+				if (cudaMemsetAsync(sync.queue, 0, sync_bytes(n), stream) != cudaSuccess) {
+					return release(cuda_fail(cudaGetLastError(), "autotune: clear queue"));
+				}
+				cudaEventRecord(t0, stream);
+				st = launch_batch_persistent(d_images, d_items, T, 4, sync, status, bps * sms, b->smem, stream);
+				if (st) return release(st);
+				cudaEventRecord(t1, stream);
+				IANE_GB_CUDA(cudaEventSynchronize(t1), "autotune: time");
+				float e = 0.0f;
+				cudaEventElapsedTime(&e, t0, t1);
+				if (rep > 0) ms += e / 2.0f; // the first run warms up
+			}
+			timings << ms << ' ';
+			if (best == 0.0f || ms < best) {
+				best = ms;
+				b->blocks_per_sm = bps;
+				b->order = order;
+			}
+		}
+	}
+	cache.choice[key] = {b->blocks_per_sm, b->order};
+	std::ofstream log(cache.path, std::ios::app);
+	if (log) log << key << " | " << timings.str() << "| " << b->blocks_per_sm << ' ' << b->order << "\n";
+	return release(IANE_GB_OK);
 }
 
 }  // namespace
@@ -427,15 +447,11 @@ int iane_gb_rl_batch_destroy(iane_gb_rl_batch* b)
 {
 	if (!b) return IANE_GB_OK;
 	for (auto* p : b->plans) iane_gb_rl_destroy(p);
-	for (int g = 0; g < kBatchGroups; ++g) cudaFree(b->d_items[g]);
+	cudaFree(b->d_items);
 	cudaFree(b->d_images);
 	cudaFree(b->d_init);
 	if (b->exec) cudaGraphExecDestroy(b->exec);
-	if (b->fork) cudaEventDestroy(b->fork);
-	for (int g = 0; g < kBatchGroups; ++g) {
-		if (b->join[g]) cudaEventDestroy(b->join[g]);
-		if (b->side[g]) cudaStreamDestroy(b->side[g]);
-	}
+	if (b->capture) cudaStreamDestroy(b->capture);
 	delete b;
 	return IANE_GB_OK;
 }
@@ -470,16 +486,7 @@ int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t*
 		b->kx.push_back(psfs[i].extent[0]);
 		b->ky.push_back(psfs[i].extent[1]);
 		b->pitch.push_back((static_cast<long long>(ext[0]) + 3) & ~3LL);
-	}
-	// tile shape per image: the tuner's cached (or freshly measured) choice, else 64x64 tiles
-	// for images at least 48 wide and high
-	b->wx.assign(count, 2);
-	for (int i = 0; i < count; ++i) {
-		if (b->nx[i] < 48 || b->ny[i] < 48) b->wx[i] = 1;
-	}
-	if (flags & IANE_GB_BATCH_AUTOTUNE) {
-		const int st = batch_autotune(b->nx, b->ny, b->kx, b->ky, b->plans, b->wx, static_cast<cudaStream_t>(stream));
-		if (st) return cleanup(st);
+		b->smem = std::max(b->smem, batch_tile_smem(psfs[i].extent[0], psfs[i].extent[1]));
 	}
 	size_t off = 0;
 	for (int i = 0; i < count; ++i) {
@@ -490,29 +497,26 @@ int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t*
 	}
 	b->parts_off = off;
 	off += align_up(static_cast<size_t>(count) * sizeof(float));
-	b->counter_off = off;
-	off += align_up(static_cast<size_t>(2 * kBatchGroups * (kMaxBatchIterations + 1)) * sizeof(unsigned int));
+	b->sync_off = off;
+	off += align_up(sync_bytes(count));
 	b->scratch_bytes = off + kAlignB;
-	fill_items(b);
-	for (int g = 0; g < kBatchGroups; ++g) {
-		if (b->items[g].empty()) continue;
-		b->grid[g] = occupancy_grid(1 + (g & 1), (g & 2) != 0, b->smem[g], b->items[g].size());
-		if (cudaMalloc(&b->d_items[g], b->items[g].size() * sizeof(BatchItem)) != cudaSuccess ||
-		    cudaMemcpy(b->d_items[g], b->items[g].data(), b->items[g].size() * sizeof(BatchItem),
-		        cudaMemcpyHostToDevice) != cudaSuccess) {
-			return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: upload work items"));
-		}
-	}
-	if (cudaMalloc(&b->d_images, count * sizeof(BatchImage)) != cudaSuccess ||
+	b->blocks_per_sm = batch_blocks_per_sm(b->smem);
+	b->order = kOrderLargestFirst;
+	b->items = make_items(b->nx, b->ny, b->kx, b->order);
+	if (cudaMalloc(&b->d_items, b->items.size() * sizeof(BatchItem)) != cudaSuccess ||
+	    cudaMalloc(&b->d_images, count * sizeof(BatchImage)) != cudaSuccess ||
 	    cudaMalloc(&b->d_init, count * sizeof(InitDesc)) != cudaSuccess ||
-	    cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+	    cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking) != cudaSuccess) {
 		return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: allocate descriptors"));
 	}
-	for (int g = 0; g < kBatchGroups; ++g) {
-		if (cudaStreamCreateWithFlags(&b->side[g], cudaStreamNonBlocking) != cudaSuccess ||
-		    cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming) != cudaSuccess) {
-			return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: allocate streams"));
-		}
+	if (flags & IANE_GB_BATCH_AUTOTUNE) {
+		const int st = autotune(b, static_cast<cudaStream_t>(stream));
+		if (st) return cleanup(st);
+		b->items = make_items(b->nx, b->ny, b->kx, b->order);
+	}
+	if (cudaMemcpy(b->d_items, b->items.data(), b->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) !=
+	    cudaSuccess) {
+		return cleanup(cuda_fail(cudaGetLastError(), "rl_batch_prepare: upload work items"));
 	}
 	*out = b;
 	return IANE_GB_OK;
@@ -526,7 +530,15 @@ size_t iane_gb_rl_batch_scratch_bytes(const iane_gb_rl_batch* b)
 int iane_gb_rl_batch_tiles(const iane_gb_rl_batch* b, int32_t* tile_width)
 {
 	if (!b || !tile_width) return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_tiles: null argument");
-	for (int i = 0; i < b->count; ++i) tile_width[i] = 32 * b->wx[i];
+	for (int i = 0; i < b->count; ++i) tile_width[i] = kBatchTile;
+	return IANE_GB_OK;
+}
+
+int iane_gb_rl_batch_config(const iane_gb_rl_batch* b, int32_t* blocks_per_sm, int32_t* order)
+{
+	if (!b || !blocks_per_sm || !order) return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_config: null argument");
+	*blocks_per_sm = b->blocks_per_sm;
+	*order = b->order;
 	return IANE_GB_OK;
 }
 
@@ -538,6 +550,9 @@ int iane_gb_rl_batch_run(iane_gb_rl_batch* b, const iane_gb_view* observed, cons
 	}
 	if (iterations < 0 || iterations > kMaxBatchIterations || !(epsilon > 0.0f) || !std::isfinite(epsilon)) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "Iterations and finite epsilon must be positive");
+	}
+	if (static_cast<long long>(b->items.size()) * 2 * iterations >= (1LL << 31)) {
+		return fail(IANE_GB_UNSUPPORTED, "rl_batch_run: more than 2^31 work items (tiles x passes)");
 	}
 	if (init < IANE_GB_RL_INIT_OBSERVED || init > IANE_GB_RL_INIT_GIVEN) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_run: unknown init mode");

@@ -1,14 +1,23 @@
 // Batched Richardson-Lucy over many images of uneven size, each with its own PSF.
 //
-// Each pass of an iteration is one persistent launch per tile shape and PSF width class (the
-// groups): the grid is a few CTAs
-// per SM and every CTA pulls work items -- (image, tile) pairs sorted by PSF width -- from
-// a device queue (an atomic counter over the item list) and runs the tiled FP32 convolution
-// body with that image's TMA map, kernel and fused epilogue. Items of one image wait for
-// nothing: a pass's launch starts only after the previous pass's launch has finished (stream
-// order inside the CUDA graph), which is the only dependency RL has. The whole schedule --
-// start values, then for every iteration pass A and pass B for the four groups on four
-// graph branches -- is captured once into a CUDA graph and replayed by later runs.
+// The whole run -- every pass of every iteration of every image -- is ONE persistent launch
+// over a device work queue. The queue is the list of (image, 64x64 tile) items of one pass,
+// repeated once per phase (phase 2t = pass A of iteration t, 2t + 1 = pass B); item k is
+// (phase k / T, entry k % T) for T items per pass. CTAs (a few per SM) take items from an
+// atomic counter in queue order and run the tiled FP32 convolution body with that image's TMA
+// map, PSF and fused epilogue. RL's only dependency is per image: a phase of an image reads
+// (with a halo) what the image's previous phase wrote and overwrites what it read, so an item
+// of phase p waits until all tiles of its image's phase p - 1 are done -- a per-image
+// completion counter that reaches p * tiles -- instead of a grid-wide drain between passes.
+// Images of the next phase start as soon as their own previous pass is complete.
+//
+// Progress: an item waits only for items earlier in the queue, which were handed to CTAs that
+// are running, so the earliest unfinished item can always proceed. Every wait is bounded (two
+// seconds of global time); a wait that gives up records IANE_GB_DEVICE_TIMEOUT in the status
+// word and raises an abort flag that every other wait checks, so the launch ends promptly.
+//
+// The CUDA graph of a run holds the counter reset, the start values and that one launch; it is
+// captured on the first run and replayed while the views, scratch and parameters are unchanged.
 #pragma once
 
 #include "rl.cuh"
@@ -16,6 +25,9 @@
 #include <vector>
 
 namespace iane_gb {
+
+// Tile edge of every work item (64 x 64 outputs; the body is 2 x 2 warps of 32 x 32).
+constexpr int kBatchTile = 64;
 
 // Device-side description of one image of the batch (64-byte aligned for the maps).
 struct alignas(64) BatchImage {
@@ -27,43 +39,37 @@ struct alignas(64) BatchImage {
 	EpiUpdate epi_b;       // write_out is set only in the last iteration (write_out_final)
 	int kx;
 	int tiles_x;
+	int tiles;             // items of this image per phase
 	int write_out_final;
-	int pad_;
 };
-
-// PSF width classes: narrow kernels (kx <= 15) take far fewer registers and less shared
-// memory than wide ones (17..31), so each class has its own kernel and the narrow one fits
-// more blocks per SM. Work items form four groups: (tile shape, width class).
-inline bool batch_wide(int kx) { return kx > 15; }
-constexpr int kBatchGroups = 4;
-inline int batch_group(int wx, int kx) { return (wx - 1) + 2 * (batch_wide(kx) ? 1 : 0); }
 
 struct BatchItem {
 	int image;
 	int tile;
 };
 
-// Persistent pass kernels (rl_batch_pass.cu). wx = wy = 1 (32x32 tiles) or 2 (64x64); wide:
-// the items' PSFs are 17..31 wide (else 1..15).
-int launch_batch_pass(int wx, bool wide, bool pass_b, const BatchImage* images, const BatchItem* items, int count,
-	unsigned int* counter, int last, int grid, size_t smem, cudaStream_t stream);
+// Device words of a run, cleared before the launch: the queue counter, the abort flag and one
+// completion counter per image.
+struct BatchSync {
+	unsigned int* queue;
+	int* abort;
+	unsigned int* done;
+};
 
-// Largest dynamic shared memory a pass of this tile shape needs for PSF width kx, height ky.
-size_t batch_tile_smem(int wx, int kx, int ky);
+// The persistent launch (rl_batch_kernel.cu): `grid` CTAs of 128 threads, `smem` bytes of
+// dynamic shared memory (batch_tile_smem over the batch), items * phases work items.
+int launch_batch_persistent(const BatchImage* images, const BatchItem* items, int items_per_phase, int phases,
+	BatchSync sync, int* status, int grid, size_t smem, cudaStream_t stream);
 
-// The pass-B kernel of a tile shape and width class (the larger register footprint), for
-// occupancy queries.
-const void* batch_kernel_handle(int wx, bool wide);
+// Dynamic shared memory a tile of PSF width kx, height ky needs.
+size_t batch_tile_smem(int kx, int ky);
+
+// Resident CTAs per SM of the persistent kernel with `smem` bytes of dynamic shared memory.
+int batch_blocks_per_sm(size_t smem);
 
 // Fill the plan-dependent fields of one image's pass arguments and epilogues (rl.cu); the
 // caller sets the buffer pointers, views and epsilon.
 void rl_plan_fill_passes(const iane_gb_rl_plan* plan, TileArgs* pass_a, TileArgs* pass_b, EpiRatio* epi_a,
 	EpiUpdate* epi_b, int* status);
-
-// Choose the tile shape (wx = 1: 32x32, 2: 64x64) of every image by timing both shapes on a
-// GPU-filling batch of copies of that image, once per (shape, PSF size, dtype, SM count);
-// choices persist in the tuning cache file.
-int batch_autotune(const std::vector<int>& nx, const std::vector<int>& ny, const std::vector<int>& kx,
-	const std::vector<int>& ky, const std::vector<iane_gb_rl_plan*>& plans, std::vector<int>& wx, cudaStream_t stream);
 
 }  // namespace iane_gb

@@ -1,0 +1,171 @@
+// The persistent kernel of the batched Richardson-Lucy run (rl_batch.cuh): one launch takes
+// every (phase, image, tile) item of the run from a device queue, waits for the item's image
+// to finish its previous phase, runs the fused tiled convolution body of the item's pass and
+// PSF width, and counts the tile as done for its image.
+#include "rl_batch.cuh"
+
+namespace iane_gb {
+namespace {
+
+// Bytes after the tiles and taps: the two tile mbarriers and the item index.
+constexpr size_t kBatchTail = 32;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned int load_acquire(const unsigned int* p)
+{
+	unsigned int v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ int load_volatile(const int* p)
+{
+	return *reinterpret_cast<const volatile int*>(p);
+}
+
+// Generic-proxy writes of this thread (the epilogue's stores) ordered against async-proxy (TMA)
+// accesses to global memory: used after a tile's stores and before a dependent tile's loads.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+	asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Thread 0: wait until image `image` has completed `need` tiles. False if the run is aborted or
+// the wait gave up (which it records and turns into an abort).
+__device__ bool wait_for_image(const BatchSync& sync, int image, unsigned int need, int* status)
+{
+	if (load_acquire(&sync.done[image]) >= need) {
+		return true;
+	}
+	const uint64_t t0 = global_ns();
+	for (uint32_t i = 1; i < (1u << 26); ++i) {
+		if (load_acquire(&sync.done[image]) >= need) {
+			return true;
+		}
+		if (load_volatile(sync.abort)) {
+			return false;
+		}
+		if ((i & 63u) == 0 && global_ns() - t0 > kWaitLimitNs) {
+			break;
+		}
+		__nanosleep(128);
+	}
+	report_device_status(status, IANE_GB_DEVICE_TIMEOUT);
+	atomicExch(sync.abort, 1);
+	return false;
+}
+
+template<bool PASS_B, class Epi>
+__device__ __forceinline__ void run_item(const BatchImage& im, Epi& epi, int x0, int y0, uint32_t& phases, uint64_t* bars)
+{
+	const CUtensorMap* map = PASS_B ? &im.map_ratio : &im.map_est;
+	const TileArgs& a = PASS_B ? im.pass_b : im.pass_a;
+#define IANE_GB_BATCH_KX(K) \
+	case K: conv_tile_body<K, 2, 2, kTileTma, Epi, true>(map, a, epi, x0, y0, 0, phases, bars); break;
+	switch (im.kx) {
+	IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
+	IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
+	IANE_GB_BATCH_KX(17) IANE_GB_BATCH_KX(19) IANE_GB_BATCH_KX(21) IANE_GB_BATCH_KX(23)
+	IANE_GB_BATCH_KX(25) IANE_GB_BATCH_KX(27) IANE_GB_BATCH_KX(29) IANE_GB_BATCH_KX(31)
+	default: break;
+	}
+#undef IANE_GB_BATCH_KX
+}
+
+// total = dynamic shared memory of the launch: the largest tile and taps + kBatchTail.
+__global__ void __launch_bounds__(128) batch_persistent_kernel(const BatchImage* __restrict__ images,
+	const BatchItem* __restrict__ items, int items_per_phase, int phases, BatchSync sync, int* status,
+	unsigned int total)
+{
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + total - kBatchTail);
+	int* shared_item = reinterpret_cast<int*>(smem_raw + total - kBatchTail + 16);
+	if (threadIdx.x == 0) {
+		mbar_init(&bars[0], 1);
+		mbar_init(&bars[1], 1);
+		fence_barrier_init();
+	}
+	const unsigned int count = static_cast<unsigned int>(items_per_phase) * static_cast<unsigned int>(phases);
+	uint32_t tile_phases = 0;
+	for (;;) {
+		__syncthreads(); // the previous item is finished everywhere; barriers initialised
+		if (threadIdx.x == 0) {
+			const unsigned int k = load_volatile(sync.abort) ? count : atomicAdd(sync.queue, 1u);
+			int go = k < count;
+			if (go) {
+				const int phase = static_cast<int>(k / static_cast<unsigned int>(items_per_phase));
+				const BatchItem w = items[k - static_cast<unsigned int>(phase) * items_per_phase];
+				if (phase > 0) {
+					go = wait_for_image(sync, w.image, static_cast<unsigned int>(phase) * images[w.image].tiles, status);
+					fence_proxy_async_global(); // the image's previous phase, written by generic stores, before TMA
+				}
+			}
+			*shared_item = go ? static_cast<int>(k) : -1;
+		}
+		__syncthreads();
+		const int k = *shared_item;
+		if (k < 0) {
+			break;
+		}
+		const int phase = k / items_per_phase;
+		const BatchItem w = items[k - phase * items_per_phase];
+		const BatchImage& im = images[w.image];
+		const int x0 = (w.tile % im.tiles_x) * kBatchTile;
+		const int y0 = (w.tile / im.tiles_x) * kBatchTile;
+		if (phase & 1) {
+			EpiUpdate epi = im.epi_b;
+			epi.want_stats = 0;
+			epi.write_out = phase == phases - 1 && im.write_out_final;
+			run_item<true>(im, epi, x0, y0, tile_phases, bars);
+		} else {
+			EpiRatio epi = im.epi_a;
+			run_item<false>(im, epi, x0, y0, tile_phases, bars);
+		}
+		fence_proxy_async_global(); // this thread's epilogue stores, before other tiles' TMA reads
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			__threadfence();
+			atomicAdd(&sync.done[w.image], 1u);
+		}
+	}
+}
+
+}  // namespace
+
+size_t batch_tile_smem(int kx, int ky)
+{
+	const int H = kBatchTile + 2 * (ky / 2);
+	const size_t plane = (static_cast<size_t>(tile_pitch(kx, 2)) * H * 4 + 127) & ~size_t(127);
+	const size_t taps = (static_cast<size_t>(ky) * ((kx + 3) & ~3) * 4 + 127) & ~size_t(127);
+	return plane + taps + 16; // 2-D images: one tile buffer and one tap buffer
+}
+
+int batch_blocks_per_sm(size_t smem)
+{
+	const size_t total = smem + kBatchTail;
+	int per_sm = 0;
+	if (cudaFuncSetAttribute(batch_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	        static_cast<int>(total)) != cudaSuccess ||
+	    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent_kernel, 128, total) != cudaSuccess) {
+		cudaGetLastError();
+		return 1;
+	}
+	return per_sm > 0 ? per_sm : 1;
+}
+
+int launch_batch_persistent(const BatchImage* images, const BatchItem* items, int items_per_phase, int phases,
+	BatchSync sync, int* status, int grid, size_t smem, cudaStream_t stream)
+{
+	if (items_per_phase <= 0 || phases <= 0) {
+		return IANE_GB_OK;
+	}
+	const size_t total = smem + kBatchTail;
+	IANE_GB_CUDA(cudaFuncSetAttribute(batch_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		static_cast<int>(total)), "batch: set shared memory size");
+	batch_persistent_kernel<<<grid, 128, total, stream>>>(images, items, items_per_phase, phases, sync, status,
+		static_cast<unsigned int>(total));
+	IANE_GB_CUDA(cudaGetLastError(), "batch: launch");
+	return IANE_GB_OK;
+}
+
+}  // namespace iane_gb

@@ -289,14 +289,17 @@ int iane_gb_wiener_destroy(iane_gb_wiener_plan* plan);
 
 /*
  * Batched Richardson-Lucy over many 2-D images of uneven size, each with its own PSF. No
- * counterpart in the reference (its example runs one image per process). Each pass of every
- * iteration is one persistent launch per tile shape over a device work queue of
- * (image, tile) items; the whole schedule is captured into a CUDA graph on the first run
- * and replayed while the views, scratch and parameters stay the same.
+ * counterpart in the reference (its example runs one image per process). The whole run --
+ * every pass of every iteration of every image -- is ONE persistent launch over a device work
+ * queue of (image, 64x64 tile) items in pass order; an image's pass waits only until that
+ * image's previous pass is complete (per-image completion counters, bounded waits), never for
+ * the rest of the batch. The run is captured into a CUDA graph on the first call and replayed
+ * while the views, scratch and parameters stay the same.
  * psfs: `count` f32 2-D device views (odd extents up to 31 x 63); extents: 2*count ints
- * (nx, ny per image). IANE_GB_BATCH_AUTOTUNE times 32x32 against 64x64 tiles per
- * (image shape, PSF size, dtype, SM count) and caches the choice in the file named by the
- * environment variable IANE_GB_TUNE_CACHE (default $HOME/.cache/iane_gb300_tune.txt).
+ * (nx, ny per image). IANE_GB_BATCH_AUTOTUNE times the launch's CTAs per SM and its queue order
+ * (largest images first, or grouped by PSF width) on this batch and caches the choice per
+ * (image shapes, PSF sizes, dtype, SM count) in the file named by the environment variable
+ * IANE_GB_TUNE_CACHE (default $HOME/.cache/iane_gb300_tune.txt).
  */
 typedef struct iane_gb_rl_batch iane_gb_rl_batch;
 #define IANE_GB_BATCH_AUTOTUNE 1u
@@ -304,8 +307,10 @@ typedef struct iane_gb_rl_batch iane_gb_rl_batch;
 int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t* extents,
 	unsigned flags, void* stream, iane_gb_rl_batch** batch);
 size_t iane_gb_rl_batch_scratch_bytes(const iane_gb_rl_batch* batch);
-/* Tile width (32 or 64) chosen for every image. */
+/* Tile width of every image's work items (64). */
 int iane_gb_rl_batch_tiles(const iane_gb_rl_batch* batch, int32_t* tile_width);
+/* The persistent launch's CTAs per SM and queue order (0: largest images first, 1: by PSF width). */
+int iane_gb_rl_batch_config(const iane_gb_rl_batch* batch, int32_t* blocks_per_sm, int32_t* order);
 /* observed / estimates: `count` views each (observed f32 or u8, estimate f32 or u8). */
 int iane_gb_rl_batch_run(iane_gb_rl_batch* batch, const iane_gb_view* observed,
 	const iane_gb_view* estimates, int iterations, float epsilon, int init, void* scratch,
