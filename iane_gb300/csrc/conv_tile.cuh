@@ -255,14 +255,15 @@ __device__ __forceinline__ void plane_sums(float (&sum)[kRY][kRX], const float* 
 	}
 }
 
-// One output tile (x0, y0, z) of the tiled convolution. Persistent kernels call it once per
+// The sums of one output tile (x0, y0, z) of the tiled convolution: acc[j][i] is the output
+// at (xo + i, yo + j, z) with (xo, yo) from tile_origin(). Persistent kernels call it once per
 // work item; `phases` carries the parity of the next wait on each tile buffer's mbarrier
-// (bit b for buffer b) from one call to the next, and `bars` are initialised by the caller.
-// The epilogue's row() runs here; its finish() is the caller's. `bars` are the two tile
-// mbarriers (TMA stages), initialised by the caller.
-template<int KX, int WX, int WY, int STAGE, class Epi, bool SINGLE = false>
-__device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, const TileArgs& a, Epi& epi, int x0,
-	int y0, int z, uint32_t& phases, uint64_t* bars)
+// (bit b for buffer b) from one call to the next, and `bars` are the two tile mbarriers (TMA
+// stages), initialised by the caller. The caller applies its epilogue to acc afterwards, so
+// none of the epilogue's state is live during the sums.
+template<int KX, int WX, int WY, int STAGE, bool SINGLE = false>
+__device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, const TileArgs& a, int x0, int y0, int z,
+	uint32_t& phases, uint64_t* bars, float (&acc)[kRY][kRX])
 {
 	using G = TileGeom<KX>;
 	constexpr int TX = 32 * WX;
@@ -289,6 +290,9 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 	const int narrow_buf = static_cast<int>(narrow_stage_bytes<KX, WX, WY>(ky, esize));
 	const int tx_b = (warp % WX) * 4 + (lane & 3);
 	const int ty_b = (warp / WX) * 8 + (lane >> 2);
+	// a warp whose 32 x 32 outputs all lie outside the image (the ragged last tiles) skips the
+	// sums: the epilogue stores nothing there, so no result changes
+	const bool warp_active = x0 + 32 * (warp % WX) < a.nx && y0 + 32 * (warp / WX) < a.ny;
 
 	// Kernel planes that touch the image: all of them except, for a zero border, planes
 	// whose input plane lies outside (those contribute only zero samples).
@@ -357,7 +361,7 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 		}
 	};
 
-	float acc[kRY][kRX];
+
 #pragma unroll
 	for (int j = 0; j < kRY; ++j)
 #pragma unroll
@@ -413,7 +417,9 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 		}
 		const float* tile = tiles + (p & 1) * plane_floats + (kRY * ty_b) * P + kRX * tx_b;
 		const float* kplane = psf_s + (p & 1) * psf_floats;
-		if constexpr (SINGLE) {
+		if (!warp_active) {
+			// nothing to sum
+		} else if constexpr (SINGLE) {
 			plane_sums<KX, P>(acc, tile, kplane, ry, ky);
 		} else {
 			float part[kRY][kRX];
@@ -435,16 +441,18 @@ __device__ __forceinline__ void conv_tile_body(const CUtensorMap* tmap_ptr, cons
 			load_taps(p + 2);
 		}
 	}
-
-	const int xo = x0 + kRX * tx_b;
-	const int yo = y0 + kRY * ty_b;
-#pragma unroll
-	for (int j = 0; j < kRY; ++j) {
-		epi.row(xo, yo + j, z, acc[j]);
-	}
 }
 
-// Shared memory bytes of the tile barriers (after the tiles and taps of conv_tile_body).
+// Origin of this thread's kRX x kRY outputs within the tile at (x0, y0) of a WX-warp-wide block.
+template<int WX>
+__device__ __forceinline__ void tile_origin(int x0, int y0, int& xo, int& yo)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	xo = x0 + kRX * ((warp % WX) * 4 + (lane & 3));
+	yo = y0 + kRY * ((warp / WX) * 8 + (lane >> 2));
+}
+
+// Shared memory bytes of the tile barriers (after the tiles and taps of conv_tile_sums).
 template<int KX, int WX, int WY>
 __device__ __forceinline__ uint64_t* tile_barriers(int ky, int kz)
 {
@@ -458,7 +466,7 @@ __device__ __forceinline__ uint64_t* tile_barriers(int ky, int kz)
 
 template<int KX, int WX, int WY, int STAGE, class Epi, bool SINGLE>
 __global__ void __launch_bounds__(32 * WX * WY)
-	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const Epi epi_in)
+	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const __grid_constant__ Epi epi_in)
 {
 	if constexpr (STAGE != kTileCopy) {
 		if (threadIdx.x == 0) {
@@ -468,10 +476,19 @@ __global__ void __launch_bounds__(32 * WX * WY)
 			fence_barrier_init();
 		}
 	}
-	Epi epi = epi_in;
 	uint32_t phases = 0;
-	conv_tile_body<KX, WX, WY, STAGE, Epi, SINGLE>(&tmap, a, epi, blockIdx.x * 32 * WX, blockIdx.y * 32 * WY, blockIdx.z, phases,
-		tile_barriers<KX, WX, WY>(a.ky, a.kz));
+	const int x0 = blockIdx.x * 32 * WX, y0 = blockIdx.y * 32 * WY;
+	float acc[kRY][kRX];
+	conv_tile_sums<KX, WX, WY, STAGE, SINGLE>(&tmap, a, x0, y0, blockIdx.z, phases, tile_barriers<KX, WX, WY>(a.ky, a.kz),
+		acc);
+	// the epilogue's state (pointers, Kahan sums) comes to life only after the sums
+	Epi epi = epi_in;
+	int xo = 0, yo = 0;
+	tile_origin<WX>(x0, y0, xo, yo);
+#pragma unroll
+	for (int j = 0; j < kRY; ++j) {
+		epi.row(xo, yo + j, blockIdx.z, acc[j]);
+	}
 	epi.finish();
 }
 

@@ -55,13 +55,15 @@ __device__ bool wait_for_image(const BatchSync& sync, int image, unsigned int ne
 	return false;
 }
 
-template<bool PASS_B, class Epi>
-__device__ __forceinline__ void run_item(const BatchImage& im, Epi& epi, int x0, int y0, uint32_t& phases, uint64_t* bars)
+// The sums of one item's tile for its PSF width (the epilogue is applied by the caller).
+template<bool PASS_B>
+__device__ __forceinline__ void item_sums(const BatchImage& im, int x0, int y0, uint32_t& phases, uint64_t* bars,
+	float (&acc)[kRY][kRX])
 {
 	const CUtensorMap* map = PASS_B ? &im.map_ratio : &im.map_est;
 	const TileArgs& a = PASS_B ? im.pass_b : im.pass_a;
 #define IANE_GB_BATCH_KX(K) \
-	case K: conv_tile_body<K, 2, 2, kTileTma, Epi, true>(map, a, epi, x0, y0, 0, phases, bars); break;
+	case K: conv_tile_sums<K, 2, 2, kTileTma, true>(map, a, x0, y0, 0, phases, bars, acc); break;
 	switch (im.kx) {
 	IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
 	IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
@@ -112,14 +114,21 @@ __global__ void __launch_bounds__(128) batch_persistent_kernel(const BatchImage*
 		const BatchImage& im = images[w.image];
 		const int x0 = (w.tile % im.tiles_x) * kBatchTile;
 		const int y0 = (w.tile / im.tiles_x) * kBatchTile;
+		float acc[kRY][kRX];
+		int xo = 0, yo = 0;
+		tile_origin<2>(x0, y0, xo, yo);
 		if (phase & 1) {
-			EpiUpdate epi = im.epi_b;
+			item_sums<true>(im, x0, y0, tile_phases, bars, acc);
+			EpiUpdate epi = im.epi_b; // read only after the sums: not live during them
 			epi.want_stats = 0;
 			epi.write_out = phase == phases - 1 && im.write_out_final;
-			run_item<true>(im, epi, x0, y0, tile_phases, bars);
+#pragma unroll
+			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
 		} else {
-			EpiRatio epi = im.epi_a;
-			run_item<false>(im, epi, x0, y0, tile_phases, bars);
+			item_sums<false>(im, x0, y0, tile_phases, bars, acc);
+			const EpiRatio epi = im.epi_a;
+#pragma unroll
+			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
 		}
 		fence_proxy_async_global(); // this thread's epilogue stores, before other tiles' TMA reads
 		__syncthreads();

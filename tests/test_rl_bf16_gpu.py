@@ -82,7 +82,9 @@ def test_bf16_rl_error_against_fp64_oracle(cuda):
     print(f"bf16 path: rel-L2 {err16:.3e}, max-abs {np.max(np.abs(got16 - ref)):.3e}; "
           f"f32 path: rel-L2 {err32:.3e}")
     assert err32 <= 1e-5
-    assert err16 <= 2e-2
+    # measured 2.5e-4 on GB300; the bar is about three times that, so a regression of the
+    # tensor-core path shows up here
+    assert err16 <= 8e-4, err16
     s = to_host(stats).reshape(-1, 2)
     assert np.all(np.isfinite(s)) and s[-1, 1] < s[0, 1]
     f32.close()
