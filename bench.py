@@ -210,6 +210,7 @@ def run_reference(args, rank):
         total += dt
     value = 3 * VOXELS * args.steps / total / 1e9
     sample = "one RL iteration (3 full-volume 15x15x7 convolutions incl. sensitivity) per step"
+    gpu_reference = reference_gpu_kernel(observed, psf)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
@@ -217,8 +218,42 @@ def run_reference(args, rank):
         "data": "synthetic", "config": config({"sample": sample}),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_reference_kernel": gpu_reference,
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_kernel(observed, psf, reps=3):
+    """The reference's own CUDA convolution (its visit_positions kernel with the convolve functor,
+    built from its headers into a cubin) timed on this GPU on the workload's convolution: the
+    observed volume with the 15x15x7 PSF, zero border. CUDA events, after one warm-up. None when
+    the cubin or a GPU is absent."""
+    try:
+        import torch
+
+        from oracle import ref_gpu
+    except ImportError:
+        return None
+    if not ref_gpu.available() or not torch.cuda.is_available():
+        return {"unavailable": "the reference cubin is built only where the reference's headers are"}
+    ref = ref_gpu.ReferenceConvolution()
+    src = torch.from_numpy(observed).cuda()
+    ker = torch.from_numpy(psf).cuda()
+    dst = torch.empty_like(src)
+    ref.convolve(src, ker, dst, "zero")
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        ref.convolve(src, ker, dst, "zero")
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    ref.close()
+    return {"ms_per_convolution": ms, "gvoxel_s": VOXELS / (ms / 1e3) / 1e9,
+            "kernel": "the reference's visit_positions with iane::convolve's functor (f32 views, FP64 fma per tap),"
+                      " nvcc sm_103a from its headers, one thread per voxel, 256-thread blocks",
+            "workload": "one 256x256x64 convolution with the 15x15x7 PSF, zero border"}
 
 
 def measure_hbm_legs(dev, stream, reps=20, cpu=True):

@@ -5,6 +5,9 @@
 * ``oracle/_ref/libiane_ref.so`` -- ``ref_shim.cpp`` compiled against the reference's own
   headers, read in place from the reference checkout (``IANE_REFERENCE`` or
   ``/root/reference``). Built only where that checkout exists; never copied.
+* ``oracle/_ref/ref_conv_f32_3d.cubin`` and ``.json`` -- the reference's own CUDA convolution
+  kernel (``ref_gpu.cu``) and its argument layout, also from the headers in place. A cubin is
+  device code, so unlike the host library it runs on a GPU host of another CPU architecture.
 
 Run as ``python oracle/build.py``.
 """
@@ -63,9 +66,39 @@ def build_reference(force: bool = False) -> Path | None:
     return REF_LIB
 
 
+REF_CUBIN = REF_DIR / "ref_conv_f32_3d.cubin"
+REF_LAYOUT = REF_DIR / "ref_conv_f32_3d.json"
+
+
+def build_reference_gpu(force: bool = False) -> Path | None:
+    """The reference's own CUDA convolution kernel for f32 3-D views (``ref_gpu.cu``) as a cubin
+    for sm_103a, and the byte layout of its functor argument (``ref_gpu_layout.cpp``, run here)
+    as JSON, both into ``_ref``. Built only where the reference checkout exists; the cubin is
+    device code, so it also serves a GPU host of another CPU architecture."""
+    root = reference_root()
+    if root is None:
+        return None
+    sources = [HERE / "ref_gpu.cu", HERE / "ref_gpu_types.hpp", HERE / "ref_gpu_layout.cpp"]
+    if force or _stale(REF_CUBIN, sources) or _stale(REF_LAYOUT, sources):
+        REF_DIR.mkdir(exist_ok=True)
+        inc = ["-I", str(root / "include")]
+        tmp = REF_CUBIN.with_suffix(".cubin.tmp")
+        subprocess.check_call(["nvcc", "-cubin", "-std=c++20", "--expt-relaxed-constexpr", "--expt-extended-lambda",
+                               "-gencode", "arch=compute_103a,code=sm_103a", "-O3", *inc,
+                               str(HERE / "ref_gpu.cu"), "-o", str(tmp)])
+        os.replace(tmp, REF_CUBIN)
+        probe = REF_DIR / "ref_gpu_layout"
+        subprocess.check_call(["g++", "-std=c++20", "-O0", *inc, str(HERE / "ref_gpu_layout.cpp"), "-o", str(probe)])
+        layout = subprocess.run([str(probe)], check=True, capture_output=True, text=True).stdout
+        REF_LAYOUT.write_text(layout)
+        probe.unlink()
+    return REF_CUBIN
+
+
 def main() -> int:
     print(build_oracle(force="--force" in sys.argv))
     print(build_reference(force="--force" in sys.argv) or "reference checkout absent: oracle/_ref not built")
+    print(build_reference_gpu(force="--force" in sys.argv) or "reference checkout absent: no reference cubin")
     return 0
 
 
