@@ -204,23 +204,39 @@ struct EpiRatioTc {
 		one(x + 32, y, z, p1);
 	}
 
-	// N (8 or 16) consecutive outputs x0 .. x0 + N - 1 of row y (x0 a multiple of N): vector
-	// loads and stores when the run lies inside the image and the observed row is f32 and aligned
+	// whether N consecutive outputs from x0 (a multiple of N) of row y take the vector path: the
+	// run lies inside the image and the observed row is f32 and 16-byte aligned
 	template<int N>
-	__device__ __forceinline__ void row_n(int x0, int y, int z, const float (&pr)[N]) const
+	__device__ __forceinline__ bool vector_run(int x0, int y, int z) const
+	{
+		const char* orow = obs + y * os[1] + z * os[2] + x0 * os[0];
+		return y < ny && x0 + N <= nx && !obs_u8 && os[0] == 4 && (reinterpret_cast<uintptr_t>(orow) & 15) == 0;
+	}
+
+	// The observed values the vector path of row_pre<N> needs, loaded ahead of time (callers
+	// issue them before they wait for the accumulators); nothing is read off the vector path.
+	template<int N>
+	__device__ __forceinline__ void preload(int x0, int y, int z, float (&o)[N]) const
+	{
+		if (!vector_run<N>(x0, y, z)) return;
+		const char* orow = obs + y * os[1] + z * os[2] + x0 * os[0];
+#pragma unroll
+		for (int q = 0; q < N / 4; ++q) {
+			const float4 v = *reinterpret_cast<const float4*>(orow + 16 * q);
+			o[4 * q] = v.x;
+			o[4 * q + 1] = v.y;
+			o[4 * q + 2] = v.z;
+			o[4 * q + 3] = v.w;
+		}
+	}
+
+	// N (8 or 16) consecutive outputs x0 .. x0 + N - 1 of row y with their observed values o
+	// from preload<N>: vector loads and stores on the vector path, one voxel at a time otherwise
+	template<int N>
+	__device__ __forceinline__ void row_pre(int x0, int y, int z, const float (&pr)[N], const float (&o)[N]) const
 	{
 		if (y >= ny) return;
-		const char* orow = obs + y * os[1] + z * os[2] + x0 * os[0];
-		if (x0 + N <= nx && !obs_u8 && os[0] == 4 && (reinterpret_cast<uintptr_t>(orow) & 15) == 0) {
-			float o[N];
-#pragma unroll
-			for (int q = 0; q < N / 4; ++q) {
-				const float4 v = *reinterpret_cast<const float4*>(orow + 16 * q);
-				o[4 * q] = v.x;
-				o[4 * q + 1] = v.y;
-				o[4 * q + 2] = v.z;
-				o[4 * q + 3] = v.w;
-			}
+		if (vector_run<N>(x0, y, z)) {
 			uint32_t w[N / 2];
 #pragma unroll
 			for (int c = 0; c < N / 2; ++c) {
@@ -236,6 +252,14 @@ struct EpiRatioTc {
 		}
 #pragma unroll
 		for (int c = 0; c < N; ++c) one(x0 + c, y, z, pr[c]);
+	}
+
+	template<int N>
+	__device__ __forceinline__ void row_n(int x0, int y, int z, const float (&pr)[N]) const
+	{
+		float o[N] = {};
+		preload<N>(x0, y, z, o);
+		row_pre<N>(x0, y, z, pr, o);
 	}
 	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&pr)[16]) const { row_n<16>(x0, y, z, pr); }
 	__device__ __forceinline__ void finish() const {}
@@ -300,22 +324,22 @@ struct EpiUpdateTc {
 		one(x + 32, y, z, c1);
 	}
 
-	// N (8 or 16) consecutive outputs x0 .. x0 + N - 1 of row y (x0 a multiple of N): vector
-	// loads and stores of the estimate and its BF16 shadow when the run lies inside the image
+	// whether N consecutive outputs from x0 (a multiple of N) of row y take the vector path: the
+	// run lies inside the image and no final copy to the caller's view is due
 	template<int N>
-	__device__ __forceinline__ void row_n(int x0, int y, int z, const float (&cv)[N])
+	__device__ __forceinline__ bool vector_run(int x0, int y) const
 	{
-		if (y >= ny) return;
-		if (x0 + N > nx || write_out) {
-#pragma unroll
-			for (int c = 0; c < N; ++c) one(x0 + c, y, z, cv[c]);
-			return;
-		}
-		const bool rows_in = y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
-		const bool all_in = rows_in && x0 >= ilo[0] && x0 + N - 1 <= ihi[0];
-		const int cyz = cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
-		float* e = est + z * plane + y * pitch + x0;  // rows are 16-byte aligned, x0 % 8 == 0
-		float old[N];
+		return y < ny && x0 + N <= nx && !write_out;
+	}
+
+	// The old estimate values the vector path of row_pre<N> needs, loaded ahead of time
+	// (callers issue them before they wait for the accumulators; the thread alone owns these
+	// voxels); nothing is read off the vector path.
+	template<int N>
+	__device__ __forceinline__ void preload(int x0, int y, int z, float (&old)[N]) const
+	{
+		if (!vector_run<N>(x0, y)) return;
+		const float* e = est + z * plane + y * pitch + x0;  // rows are 16-byte aligned, x0 % 8 == 0
 #pragma unroll
 		for (int q = 0; q < N / 4; ++q) {
 			const float4 v = reinterpret_cast<const float4*>(e)[q];
@@ -324,6 +348,24 @@ struct EpiUpdateTc {
 			old[4 * q + 2] = v.z;
 			old[4 * q + 3] = v.w;
 		}
+	}
+
+	// N (8 or 16) consecutive outputs x0 .. x0 + N - 1 of row y with their old estimate values
+	// from preload<N>: vector stores of the estimate and its BF16 shadow on the vector path, one
+	// voxel at a time otherwise
+	template<int N>
+	__device__ __forceinline__ void row_pre(int x0, int y, int z, const float (&cv)[N], const float (&old)[N])
+	{
+		if (y >= ny) return;
+		if (!vector_run<N>(x0, y)) {
+#pragma unroll
+			for (int c = 0; c < N; ++c) one(x0 + c, y, z, cv[c]);
+			return;
+		}
+		const bool rows_in = y >= ilo[1] && y <= ihi[1] && z >= ilo[2] && z <= ihi[2];
+		const bool all_in = rows_in && x0 >= ilo[0] && x0 + N - 1 <= ihi[0];
+		const int cyz = cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
+		float* e = est + z * plane + y * pitch + x0;
 		float upd[N];
 #pragma unroll
 		for (int c = 0; c < N; ++c) {
@@ -351,6 +393,14 @@ struct EpiUpdateTc {
 		uint4* d16 = reinterpret_cast<uint4*>(est16 + z * plane16 + y * pitch16 + x0);
 #pragma unroll
 		for (int q = 0; q < N / 8; ++q) d16[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+	}
+
+	template<int N>
+	__device__ __forceinline__ void row_n(int x0, int y, int z, const float (&cv)[N])
+	{
+		float old[N] = {};
+		preload<N>(x0, y, z, old);
+		row_pre<N>(x0, y, z, cv, old);
 	}
 	__device__ __forceinline__ void row16(int x0, int y, int z, const float (&cv)[16]) { row_n<16>(x0, y, z, cv); }
 

@@ -23,7 +23,7 @@
 // commits plane i to its own mbarrier; eight epilogue warps (one TMEM lane = one output row,
 // two warps per lane quarter, each taking 8 of the plane's 16 columns) finish plane i meanwhile
 // -- read its columns and hand each thread's 8 voxels to the pass epilogue (EpiRatioTc /
-// EpiUpdateTc row_n<8>: vector loads and stores) -- so the epilogue of the early planes
+// EpiUpdateTc row_pre<8>: vector loads issued a plane ahead, vector stores) -- so the epilogue of the early planes
 // overlaps the MMAs of the later ones.
 #pragma once
 
@@ -172,12 +172,21 @@ __global__ void __launch_bounds__(kTczThreads) tcz_conv_kernel(const __grid_cons
 	}
 	// Epilogue (warps 0-3 and 5-8), one output plane at a time as its accumulators become
 	// final: the thread holds row y0 + 32 (warp % 4) + lane and 8 consecutive columns of it
-	// and finishes them with 16-byte loads and stores.
+	// and finishes them with 16-byte loads and stores. The memory operand of plane i + 1 (the
+	// observed row, or the old estimate) is loaded before the wait for plane i, so its latency
+	// overlaps the MMAs instead of following them.
 	Epi epi = epi_in;
 	if (warp != 4) {
 		const int quarter = warp & 3, half = warp > 4 ? 1 : 0;
 		const uint32_t lanes = static_cast<uint32_t>(32 * quarter) << 16;
+		const int ex = x0 + 8 * half, ey = y0 + 32 * quarter + lane;
+		float next[8] = {};
+		if (nout > 0) epi.template preload<8>(ex, ey, Z, next);
 		for (int i = 0; i < nout; ++i) {
+			float cur[8];
+#pragma unroll
+			for (int c = 0; c < 8; ++c) cur[c] = next[c];
+			if (i + 1 < nout) epi.template preload<8>(ex, ey, Z + i + 1, next);
 			if (!mbar_wait_bounded(&plane_bar[i], 0)) {
 				report_device_status(a.status, IANE_GB_DEVICE_TIMEOUT);
 			}
@@ -185,7 +194,7 @@ __global__ void __launch_bounds__(kTczThreads) tcz_conv_kernel(const __grid_cons
 			tc::fence_after_sync();
 			float v[8];
 			tc::ld_32x32b_x8(tmem + lanes + 16 * i + 8 * half, v);
-			epi.template row_n<8>(x0 + 8 * half, y0 + 32 * quarter + lane, Z + i, v);
+			epi.template row_pre<8>(ex, ey, Z + i, v, cur);
 		}
 	}
 	tc::fence_before_sync();
