@@ -4,11 +4,11 @@ Architecture (3 levels, 16/32/64 channels, 3x3x3 convolutions, ReLU, average poo
 nearest upsampling, skip connections by channel concatenation, residual head):
 
     input  [2]: observed / mean(observed), PSF sigma / 3 (constant channel)
-    e1a 2->16, e1b 16->16 | pool | e2a 16->32, e2b 32->32 | pool | e3a 32->64, e3b 64->64
-    up | d2a (64+32)->32, d2b 32->32 | up | d1a (32+16)->16, d1b 16->16 | head 16->1
+    e1a 2->16, e1b 16->16 | pool | e2a 16->32, e2b 32->32 | pool | e3a 32->64, e3b 64->64,
+    e3c 64->64 | up | d2a (64+32)->32, d2b 32->32 | up | d1a (32+16)->16, d1b 16->16 | head 16->1
     output = observed / mean + head  (times the mean: the RL start, floored at eps)
 
-About 0.36 M parameters. Activations and weights are BF16, accumulation FP32, master weights
+464,785 parameters (about 0.46 M). Activations and weights are BF16, accumulation FP32, master weights
 FP32 with Adam. Every operation runs in libiane_gb300.so (iane_gb_cnn_*); torch supplies
 device memory only. Training pairs are generated here: ellipsoid phantoms blurred by random
 Gaussian PSFs with Poisson noise, paired with long FP32 Richardson-Lucy runs of this library.
@@ -28,7 +28,7 @@ LAYERS = [
     # name, input channels, output channels, relu
     ("e1a", 2, 16, True), ("e1b", 16, 16, True),
     ("e2a", 16, 32, True), ("e2b", 32, 32, True),
-    ("e3a", 32, 64, True), ("e3b", 64, 64, True),
+    ("e3a", 32, 64, True), ("e3b", 64, 64, True), ("e3c", 64, 64, True),
     ("d2a", 96, 32, True), ("d2b", 32, 32, True),
     ("d1a", 48, 16, True), ("d1b", 16, 16, True),
     ("head", 16, 1, False),
@@ -106,7 +106,8 @@ class WarmStartNet:
         s1, s2, s3 = (d, h, w), (d // 2, h // 2, w // 2), (d // 4, h // 4, w // 4)
         b = {"x16": self._act(2, s1)}
         for name, c, s in (("e1a", 16, s1), ("e1b", 16, s1), ("p1", 16, s2), ("e2a", 32, s2), ("e2b", 32, s2),
-                           ("p2", 32, s3), ("e3a", 64, s3), ("e3b", 64, s3), ("u2", 64, s2), ("d2a", 32, s2),
+                           ("p2", 32, s3), ("e3a", 64, s3), ("e3b", 64, s3), ("e3c", 64, s3), ("u2", 64, s2),
+                           ("d2a", 32, s2),
                            ("d2b", 32, s2), ("u1", 32, s1), ("d1a", 16, s1), ("d1b", 16, s1)):
             b[name] = self._act(c, s)
         b["out"] = torch.empty((1,) + s1, dtype=torch.float32, device=self.device)
@@ -206,7 +207,8 @@ class WarmStartNet:
         check(lib().iane_gb_cnn_pool2(_p(b["e2b"]), 32, *s2, _p(b["p2"]), st))
         c("e3a", b["p2"], 32, None, 0, s3, 64, y16=b["e3a"])
         c("e3b", b["e3a"], 64, None, 0, s3, 64, y16=b["e3b"])
-        check(lib().iane_gb_cnn_up2(_p(b["e3b"]), 64, *s3, _p(b["u2"]), st))
+        c("e3c", b["e3b"], 64, None, 0, s3, 64, y16=b["e3c"])
+        check(lib().iane_gb_cnn_up2(_p(b["e3c"]), 64, *s3, _p(b["u2"]), st))
         c("d2a", b["u2"], 64, b["e2b"], 32, s2, 32, y16=b["d2a"])
         c("d2b", b["d2a"], 32, None, 0, s2, 32, y16=b["d2b"])
         check(lib().iane_gb_cnn_up2(_p(b["d2b"]), 32, *s2, _p(b["u1"]), st))
@@ -253,12 +255,14 @@ class WarmStartNet:
         g_cat2 = b["g_cat2"].view(-1)
         c(b["g32b"], 32, None, 0, s2, fd2a[: 64 * 32 * 27], None, 64, y16=g_cat2[: 64 * vol2], relu=False)
         c(b["g32b"], 32, None, 0, s2, fd2a[64 * 32 * 27:], None, 32, y16=g_cat2[64 * vol2:], relu=False)
-        # up2 -> e3b, e3a
-        check(lib().iane_gb_cnn_up2_grad(_p(g_cat2[: 64 * vol2]), 64, *s3, _p(b["g64a"]), _p(b["e3b"]), st))
-        self._wgrad(b, b["e3a"], 64, None, 0, s3, b["g64a"], 64, "e3b")
-        c(b["g64a"], 64, None, 0, s3, f["e3b"], None, 64, y16=b["g64b"], relu=False, mask=b["e3a"])
-        self._wgrad(b, b["p2"], 32, None, 0, s3, b["g64b"], 64, "e3a")
-        c(b["g64b"], 64, None, 0, s3, f["e3a"], None, 32, y16=b["g_p2"], relu=False)
+        # up2 -> e3c, e3b, e3a
+        check(lib().iane_gb_cnn_up2_grad(_p(g_cat2[: 64 * vol2]), 64, *s3, _p(b["g64a"]), _p(b["e3c"]), st))
+        self._wgrad(b, b["e3b"], 64, None, 0, s3, b["g64a"], 64, "e3c")
+        c(b["g64a"], 64, None, 0, s3, f["e3c"], None, 64, y16=b["g64b"], relu=False, mask=b["e3b"])
+        self._wgrad(b, b["e3a"], 64, None, 0, s3, b["g64b"], 64, "e3b")
+        c(b["g64b"], 64, None, 0, s3, f["e3b"], None, 64, y16=b["g64a"], relu=False, mask=b["e3a"])
+        self._wgrad(b, b["p2"], 32, None, 0, s3, b["g64a"], 64, "e3a")
+        c(b["g64a"], 64, None, 0, s3, f["e3a"], None, 32, y16=b["g_p2"], relu=False)
         # pool2 -> e2b (adds the skip gradient already in g_cat2[64:96], ReLU mask)
         g_e2b = g_cat2[64 * vol2:]
         check(lib().iane_gb_cnn_pool2_grad(_p(b["g_p2"]), 32, *s2, _p(g_e2b), _p(b["e2b"]), 1, st))

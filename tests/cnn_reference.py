@@ -12,6 +12,7 @@ import torch.nn.functional as F
 
 LAYERS = [
     ("e1a", 2, 16), ("e1b", 16, 16), ("e2a", 16, 32), ("e2b", 32, 32), ("e3a", 32, 64), ("e3b", 64, 64),
+    ("e3c", 64, 64),
     ("d2a", 96, 32), ("d2b", 32, 32), ("d1a", 48, 16), ("d1b", 16, 16), ("head", 16, 1),
 ]
 
@@ -78,7 +79,8 @@ def forward(p, x, residual, round_activations=True):
     p2 = R(pool2(e2b))
     e3a = layer("e3a", p2)
     e3b = layer("e3b", e3a)
-    d2a = layer("d2a", torch.cat([up2(e3b), e2b], 0))
+    e3c = layer("e3c", e3b)
+    d2a = layer("d2a", torch.cat([up2(e3c), e2b], 0))
     d2b = layer("d2b", d2a)
     d1a = layer("d1a", torch.cat([up2(d2b), e1b], 0))
     d1b = layer("d1b", d1a)
