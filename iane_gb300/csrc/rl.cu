@@ -111,15 +111,19 @@ __global__ void rl_mean_kernel(DevView obs, double* partials, unsigned int* coun
 {
 	const int nx = obs.ext[0], ny = obs.ext[1], nz = obs.ext[2];
 	const long long n = static_cast<long long>(nx) * ny * nz;
+	// every warp takes whole rows (one index division per row, none per voxel), lanes stride x
+	const int lane = threadIdx.x & 31;
+	const long long warps = static_cast<long long>(gridDim.x) * (blockDim.x >> 5);
+	const bool u8 = obs.dtype == IANE_GB_U8;
 	double s = 0.0;
-	for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-	     i += static_cast<long long>(gridDim.x) * blockDim.x) {
-		const int x = static_cast<int>(i % nx);
-		const int y = static_cast<int>((i / nx) % ny);
-		const int z = static_cast<int>(i / (static_cast<long long>(nx) * ny));
-		const char* p = obs.ptr + x * obs.stride[0] + y * obs.stride[1] + z * obs.stride[2];
-		s += obs.dtype == IANE_GB_U8 ? static_cast<double>(*reinterpret_cast<const uint8_t*>(p))
-			: static_cast<double>(*reinterpret_cast<const float*>(p));
+	for (long long r = blockIdx.x * static_cast<long long>(blockDim.x >> 5) + (threadIdx.x >> 5);
+	     r < static_cast<long long>(ny) * nz; r += warps) {
+		const int y = static_cast<int>(r % ny), z = static_cast<int>(r / ny);
+		const char* row = obs.ptr + y * obs.stride[1] + z * obs.stride[2];
+		for (int x = lane; x < nx; x += 32) {
+			const char* p = row + x * obs.stride[0];
+			s += u8 ? static_cast<double>(*reinterpret_cast<const uint8_t*>(p)) : static_cast<double>(*reinterpret_cast<const float*>(p));
+		}
 	}
 	__shared__ double red[32];
 	__shared__ int last;
