@@ -35,6 +35,10 @@ int launch_conv_separable_fast(const DevView& src, const DevView* taps, const De
 	cudaStream_t stream);
 
 // Fused separable FP32 convolution, any tap length (separable.cu).
+// Large 2-D f32 images (separable_rows.cu): IANE_GB_UNSUPPORTED when the view or radius does
+// not qualify.
+int launch_separable_rows(const DevView& src, const DevView* taps, const DevView& dst, int border,
+	cudaStream_t stream);
 int launch_conv_separable(const DevView& src, const DevView* taps, const DevView& dst, int border,
 	cudaStream_t stream);
 

@@ -618,6 +618,11 @@ int launch_conv_separable_fast(const DevView& src, const DevView* taps, const De
 	if (src.stride[0] != 4 || r > 7 || src.ext[1] > 65535 * kFY || src.ext[2] > 65535 * 64) {
 		return IANE_GB_UNSUPPORTED;
 	}
+	// large 2-D images stream down row strips (separable_rows.cu)
+	const int rows = launch_separable_rows(src, taps, dst, border, stream);
+	if (rows != IANE_GB_UNSUPPORTED) {
+		return rows;
+	}
 	switch (r) {
 	case 0:
 	case 1: return launch_radius<1>(src, taps, dst, border, stream);
