@@ -21,6 +21,7 @@
 #include "kernels.h"
 
 #include <algorithm>
+#include <cmath>
 
 namespace iane_gb {
 namespace {
@@ -584,7 +585,27 @@ int launch_radius(const DevView& src, const DevView* taps, const DevView& dst, i
 			const size_t rsmem = RingGeom<R>::BYTES;
 			IANE_GB_CUDA(cudaFuncSetAttribute(separable_ring_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 				static_cast<int>(rsmem)), "separable: set shared memory size");
-			separable_ring_kernel<R><<<grid, kFThreads, rsmem, stream>>>(map, a);
+			// z chunks per column: the count that maximises the busy fraction of the last wave
+			// times the share of planes that are not the chunk's 2R halo, from at least one wave
+			int per_sm = 1;
+			cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, separable_ring_kernel<R>, kFThreads, rsmem);
+			const double slots = static_cast<double>(std::max(per_sm, 1)) * sms;
+			int best_chunk = chunk;
+			double best = -1.0;
+			for (int c = 1; c <= a.nz && c <= 256; ++c) {
+				const int len = (a.nz + c - 1) / c;
+				if (len < 2 * G::K) break;
+				const double waves = static_cast<double>(columns) * c / slots;
+				if (waves < 1.0) continue;
+				const double score = waves / std::ceil(waves) * len / (len + 2.0 * R);
+				if (score > best) {
+					best = score;
+					best_chunk = len;
+				}
+			}
+			a.zchunk = best_chunk;
+			const dim3 rgrid(grid.x, grid.y, (a.nz + best_chunk - 1) / best_chunk);
+			separable_ring_kernel<R><<<rgrid, kFThreads, rsmem, stream>>>(map, a);
 			IANE_GB_CUDA(cudaGetLastError(), "separable: launch");
 			return IANE_GB_OK;
 		}
