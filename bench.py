@@ -155,13 +155,31 @@ def fp32_peak_tflops(dev):
     return _FP32_PEAK
 
 
-def cpu_sample(observed, psf, threads, iterations):
-    """The reference's RL loop (oracle port, all host threads) over the full volume: the
-    sensitivity convolution plus `iterations` iterations of two convolutions each."""
+def reference_kind() -> str:
+    """"reference" when the reference's own library (its headers compiled into oracle/_ref)
+    loads on this host, else "port" (the C restatement pinned to it). The library is built
+    where the reference's headers are; a GPU host of another CPU architecture has the port."""
     import oracle
 
+    if oracle.reference_available():
+        try:
+            oracle.ref_lib()
+            return "reference"
+        except OSError:
+            return "port"
+    return "port"
+
+
+def cpu_sample(observed, psf, threads, iterations):
+    """The reference's RL loop (its own library where it loads, else the oracle port; all host
+    threads) over the full volume: the sensitivity convolution plus `iterations` iterations of
+    two convolutions each."""
+    import oracle
+
+    use_reference = reference_kind() == "reference"
     t0 = time.perf_counter()
-    oracle.rl(observed, psf, iterations, EPSILON, init=oracle.abi.RL_INIT_MEAN, threads=threads)
+    oracle.rl(observed, psf, iterations, EPSILON, init=oracle.abi.RL_INIT_MEAN, threads=threads,
+              use_reference=use_reference)
     dt = time.perf_counter() - t0
     convs = 1 + 2 * iterations
     return convs * observed.size / dt / 1e9, dt
@@ -186,9 +204,11 @@ def job_throughput(world: int, units_per_step: float, steps: int, seconds: float
 
 
 def run_reference(args, rank):
-    """Reference arm: the reference's CPU RL path (the oracle port: the reference's own build
-    needs its headers, which are not on the GPU host), all host threads; each step is one
-    RL iteration over the full volume."""
+    """Reference arm: the reference's CPU RL path -- its own library built from its headers
+    where that loads, else the oracle port pinned to it (the headers exist only where the
+    reference checkout is, and the GPU host has another CPU architecture) -- on all host
+    threads; each step is one RL iteration over the full volume. The reference's own CUDA
+    convolution kernel is timed beside it on the GPU (`gpu_reference_kernel`)."""
     if rank != 0:
         return
     import numpy as np  # noqa: F401
@@ -216,7 +236,7 @@ def run_reference(args, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 accumulate",
         "data": "synthetic", "config": config({"sample": sample}),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": reference_kind(), "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_reference_kernel": gpu_reference,
     }
@@ -853,8 +873,10 @@ def main():
         oracle_build.build_oracle()
         threads = oracle.default_threads()
         v, dt = cpu_sample(observed, psf, threads, CPU_ITERATIONS)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"oracle RL, {CPU_ITERATIONS} iterations + sensitivity on the full volume "
+        kind = reference_kind()
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{'the reference library' if kind == 'reference' else 'oracle port'} RL, "
+                         f"{CPU_ITERATIONS} iterations + sensitivity on the full volume "
                          f"({1 + 2 * CPU_ITERATIONS} convolutions, {dt:.1f} s)"}
 
     if rank == 0:
