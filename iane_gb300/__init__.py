@@ -284,9 +284,11 @@ class RichardsonLucy:
     INIT_MEAN = abi.RL_INIT_MEAN
     INIT_GIVEN = abi.RL_INIT_GIVEN
 
-    def __init__(self, psf, shape, stream=None, precision: str = "f32"):
+    def __init__(self, psf, shape, stream=None, precision: str = "f32", per_pass: bool = False):
         """``precision="bf16"`` selects the tensor-core path: BF16 images and PSF in the
-        convolutions (tcgen05 implicit GEMM, FP32 accumulation), FP32 everything else."""
+        convolutions (tcgen05 implicit GEMM, FP32 accumulation), FP32 everything else.
+        ``per_pass=True`` makes the FP32 path launch once per pass instead of once per run
+        (same results)."""
         self.shape = tuple(int(s) for s in shape)
         self.precision = precision
         if precision not in ("f32", "bf16"):
@@ -296,6 +298,8 @@ class RichardsonLucy:
         handle = ctypes.c_void_p()
         v = _device_view(psf)
         flags = abi.RL_BF16_TENSOR if precision == "bf16" else 0
+        if per_pass:
+            flags |= abi.RL_PER_PASS
         check(lib().iane_gb_rl_prepare_ex(ctypes.byref(v), rank, ext, flags, _stream_handle(stream),
                                           ctypes.byref(handle)))
         self._plan = handle

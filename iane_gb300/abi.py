@@ -27,6 +27,7 @@ RL_INIT_OBSERVED, RL_INIT_MEAN, RL_INIT_GIVEN = 0, 1, 2
 ERODE, DILATE, OPENING, CLOSING = 0, 1, 2, 3
 MORPHOLOGY_OPS = {"erode": ERODE, "dilate": DILATE, "opening": OPENING, "closing": CLOSING}
 RL_BF16_TENSOR = 1
+RL_PER_PASS = 2
 BATCH_AUTOTUNE = 1
 
 OK = 0

@@ -312,6 +312,26 @@ __device__ __forceinline__ uint64_t global_ns()
 	return t;
 }
 
+// Acquire load of a completion counter that other CTAs release with a fence and an atomic.
+__device__ __forceinline__ unsigned int load_acquire(const unsigned int* p)
+{
+	unsigned int v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ int load_volatile(const int* p)
+{
+	return *reinterpret_cast<const volatile int*>(p);
+}
+
+// Generic-proxy writes of this thread (epilogue stores) ordered against async-proxy (TMA)
+// accesses to global memory: used after a tile's stores and before a dependent tile's loads.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+	asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // Bounded wait on an mbarrier phase: gives up (returns false) after `limit_ns` of global time
 // -- two seconds unless told otherwise -- or 2^26 tries, whichever comes first, so that a
 // phase that never completes ends the kernel instead of hanging it. The caller records the

@@ -10,10 +10,13 @@
 //            has that layout -- then the passes update it in place)
 //   parts  : 3 doubles per block of pass B (statistics partials)
 //   misc   : block-completion counter and the flat-start value
+//   sync   : queue counter, abort flag and per-plane completion counters of the persistent
+//            run (rl_persist.cuh)
 #include "kernels.h"
 #include "rl.cuh"
 #include "rl_tcz.cuh"
 #include "rl_batch.cuh"
+#include "rl_persist.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -35,8 +38,10 @@ struct iane_gb_rl_plan {
 	long long pitch;       // floats per work-image row
 	size_t image_bytes;    // one work image, rounded to 256
 	size_t parts_bytes;
+	size_t sync_bytes;     // persistent-run words (FP32 path)
 	size_t scratch_bytes;
 	bool small_tiles;
+	bool per_pass;         // IANE_GB_RL_PER_PASS: one launch per pass instead of one per run
 	long long pass_blocks;
 	// BF16 tensor-core precision path (IANE_GB_RL_BF16_TENSOR)
 	bool bf16;
@@ -64,6 +69,11 @@ int launch_rl_pass_b(int kx, bool small, const CUtensorMap& map, const TileArgs&
 	cudaStream_t stream)
 {
 	return kx <= 15 ? launch_rl_pass_b_lo(kx, small, map, a, e, stream) : launch_rl_pass_b_hi(kx, small, map, a, e, stream);
+}
+
+int launch_rl_persist(int kx, const RlPersistArgs& p, cudaStream_t stream)
+{
+	return kx <= 15 ? launch_rl_persist_lo(kx, p, stream) : launch_rl_persist_hi(kx, p, stream);
 }
 
 namespace {
@@ -535,7 +545,7 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 	iane_gb_rl_plan** out)
 {
 	const bool bf16 = (flags & IANE_GB_RL_BF16_TENSOR) != 0;
-	if (flags & ~IANE_GB_RL_BF16_TENSOR) {
+	if (flags & ~(IANE_GB_RL_BF16_TENSOR | IANE_GB_RL_PER_PASS)) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "rl_prepare: unknown flags");
 	}
 	if (!out || !extent) {
@@ -574,6 +584,7 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 	auto* plan = new iane_gb_rl_plan{};
 	plan->rank = rank;
 	plan->bf16 = bf16;
+	plan->per_pass = (flags & IANE_GB_RL_PER_PASS) != 0;
 	for (int i = 0; i < 3; ++i) {
 		plan->ext[i] = ext[i];
 		plan->k[i] = k.ext[i];
@@ -693,7 +704,8 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 	const long long mean_blocks = 8LL * device_sm_count();
 	plan->parts_bytes = round_up(static_cast<size_t>(
 		(plan->pass_blocks * 3 > mean_blocks ? plan->pass_blocks * 3 : mean_blocks) * sizeof(double)), kAlign);
-	plan->scratch_bytes = 2 * plan->image_bytes + plan->parts_bytes + 2 * kAlign;
+	plan->sync_bytes = round_up(rl_persist_sync_bytes(ext[2]), kAlign);
+	plan->scratch_bytes = 2 * plan->image_bytes + plan->parts_bytes + 2 * kAlign + plan->sync_bytes;
 	if (bf16) {
 		// scratch: f32 work estimate, bf16 estimate shadow, bf16 ratio, partials, counter
 		plan->pitch16 = (static_cast<long long>(ext[0]) + 7) & ~7LL;
@@ -782,7 +794,7 @@ int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const ia
 	}
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
 	char* base = reinterpret_cast<char*>(round_up(reinterpret_cast<uintptr_t>(scratch), kAlign));
-	if (base + (plan->scratch_bytes - 2 * kAlign) + 8 > static_cast<char*>(scratch) + scratch_bytes) {
+	if (base + (plan->scratch_bytes - kAlign) > static_cast<char*>(scratch) + scratch_bytes) {
 		return fail(IANE_GB_LENGTH_ERROR, "Prepared operation exceeded its scratch reservation");
 	}
 	if (plan->bf16) {
@@ -875,6 +887,34 @@ int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const ia
 	eb.out = est.ptr;
 	eb.out_u8 = est.dtype == IANE_GB_U8;
 
+	// One persistent launch for the whole run (rl_persist.cuh) unless the caller wants per-iteration
+	// statistics (their deterministic block-order reduction closes each pass B launch), the image is
+	// small enough for 32 x 32 tiles, or the plan asks for one launch per pass.
+	const long long tiles_x = (nx + 63) / 64, tiles_y = (ny + 63) / 64;
+	const bool persistent = !plan->per_pass && !plan->small_tiles && stats == nullptr && iterations > 0 &&
+		tiles_x * tiles_y * nz * 2LL * iterations < (1LL << 31);
+	if (persistent) {
+		unsigned int* sync = reinterpret_cast<unsigned int*>(base + 2 * plan->image_bytes + plan->parts_bytes + kAlign);
+		RlPersistArgs pa{};
+		pa.map_est = map_est;
+		pa.map_ratio = map_ratio;
+		pa.pass_a = ta;
+		pa.pass_b = tb;
+		pa.epi_a = ea;
+		eb.want_stats = 0;
+		eb.stats = nullptr;
+		eb.write_out = in_place ? 0 : 1;
+		pa.epi_b = eb;
+		pa.tiles_x = static_cast<int>(tiles_x);
+		pa.tiles_y = static_cast<int>(tiles_y);
+		pa.nz = nz;
+		pa.phases = 2 * iterations;
+		pa.queue = sync;
+		pa.abort = reinterpret_cast<int*>(sync + 1);
+		pa.done = sync + 2;
+		IANE_GB_CUDA(cudaMemsetAsync(sync, 0, rl_persist_sync_bytes(nz), st), "rl_run: clear queue");
+		return launch_rl_persist(kx, pa, st);
+	}
 	for (int it = 0; it < iterations; ++it) {
 		status = launch_rl_pass_a(kx, plan->small_tiles, map_est, ta, ea, st);
 		if (status) return status;

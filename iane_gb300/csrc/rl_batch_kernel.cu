@@ -11,25 +11,6 @@ namespace {
 constexpr size_t kBatchTail = 32;
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
-__device__ __forceinline__ unsigned int load_acquire(const unsigned int* p)
-{
-	unsigned int v;
-	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-	return v;
-}
-
-__device__ __forceinline__ int load_volatile(const int* p)
-{
-	return *reinterpret_cast<const volatile int*>(p);
-}
-
-// Generic-proxy writes of this thread (the epilogue's stores) ordered against async-proxy (TMA)
-// accesses to global memory: used after a tile's stores and before a dependent tile's loads.
-__device__ __forceinline__ void fence_proxy_async_global()
-{
-	asm volatile("fence.proxy.async.global;" ::: "memory");
-}
-
 // Thread 0: wait until image `image` has completed `need` tiles. False if the run is aborted or
 // the wait gave up (which it records and turns into an abort).
 __device__ bool wait_for_image(const BatchSync& sync, int image, unsigned int need, int* status)
