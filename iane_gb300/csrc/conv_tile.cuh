@@ -22,6 +22,12 @@
 //     cost more issue slots than the packing saves);
 //   * only the current and next kernel planes' taps are held in shared memory, so four
 //     64x64-tile blocks fit per SM.
+// A second lane geometry (template RX = 16, RY = 2: 2 x 16 lanes, each 16 x by 2 y outputs)
+// covers the same 32 x 32 per warp and reads the same tile (its width does not depend on RX):
+// per kernel row it loads the taps once for 16 x 2 = 32 FMAs per tap instead of twice, and
+// the interior input rows, which feed both output rows, run without the kernel-row checks.
+// The persistent RL kernel uses it; the sums are the same bits in either geometry (each
+// output's taps are added in the same order).
 // Per kernel plane each output accumulates its ky*kx taps into a plane partial that is
 // added to the total afterwards (two-level FP32 summation), which keeps the rounding error
 // of a 1575-tap sum near 1e-6 relative. Single-plane kernels (SINGLE) sum straight into the
@@ -212,46 +218,66 @@ __device__ __forceinline__ void convert_narrow(const unsigned char* sg, float* t
 	}
 }
 
-template<int KX, int P>
-__device__ __forceinline__ void plane_sums(float (&sum)[kRY][kRX], const float* tile, const float* kplane, int ry, int ky)
+// Input row r of the lane's window: read its segment once and apply it to every output row j
+// whose kernel row b = j + 2 ry - r exists (CHECK false: the caller knows all of them do).
+template<int KX, int P, int RX, int RY, bool CHECK>
+__device__ __forceinline__ void row_sums(float (&sum)[RY][RX], const float* tile, const float* kplane, int ry, int ky,
+	int r)
 {
 	using G = TileGeom<KX>;
-	const int rows = kRY + 2 * ry;
-#pragma unroll 1
-	for (int r = 0; r < rows; ++r) {
-		float seg[G::SEGN];
-		const float4* srow = reinterpret_cast<const float4*>(tile + r * P);
+	constexpr int SEGN = (G::D + RX + KX - 1 + 3) & ~3;
+	float seg[SEGN];
+	const float4* srow = reinterpret_cast<const float4*>(tile + r * P);
 #pragma unroll
-		for (int m = 0; m < G::SEGN / 4; ++m) {
-			const float4 v = srow[m];
-			seg[4 * m + 0] = v.x;
-			seg[4 * m + 1] = v.y;
-			seg[4 * m + 2] = v.z;
-			seg[4 * m + 3] = v.w;
-		}
+	for (int m = 0; m < SEGN / 4; ++m) {
+		const float4 v = srow[m];
+		seg[4 * m + 0] = v.x;
+		seg[4 * m + 1] = v.y;
+		seg[4 * m + 2] = v.z;
+		seg[4 * m + 3] = v.w;
+	}
 #pragma unroll
-		for (int j = 0; j < kRY; ++j) {
-			const int b = j + 2 * ry - r;
-			if (b >= 0 && b < ky) {
-				const float4* krow = reinterpret_cast<const float4*>(kplane + b * G::KXP);
-				float k[G::KXP];
+	for (int j = 0; j < RY; ++j) {
+		const int b = j + 2 * ry - r;
+		if (!CHECK || (b >= 0 && b < ky)) {
+			const float4* krow = reinterpret_cast<const float4*>(kplane + b * G::KXP);
+			float k[G::KXP];
 #pragma unroll
-				for (int m = 0; m < G::KXP / 4; ++m) {
-					const float4 v = krow[m];
-					k[4 * m + 0] = v.x;
-					k[4 * m + 1] = v.y;
-					k[4 * m + 2] = v.z;
-					k[4 * m + 3] = v.w;
-				}
+			for (int m = 0; m < G::KXP / 4; ++m) {
+				const float4 v = krow[m];
+				k[4 * m + 0] = v.x;
+				k[4 * m + 1] = v.y;
+				k[4 * m + 2] = v.z;
+				k[4 * m + 3] = v.w;
+			}
 #pragma unroll
-				for (int q = 0; q < KX; ++q) {
+			for (int q = 0; q < KX; ++q) {
 #pragma unroll
-					for (int i = 0; i < kRX; ++i) {
-						sum[j][i] = fmaf(k[q], seg[G::D + i + 2 * G::rx - q], sum[j][i]);
-					}
+				for (int i = 0; i < RX; ++i) {
+					sum[j][i] = fmaf(k[q], seg[G::D + i + 2 * G::rx - q], sum[j][i]);
 				}
 			}
 		}
+	}
+}
+
+template<int KX, int P, int RX = kRX, int RY = kRY>
+__device__ __forceinline__ void plane_sums(float (&sum)[RY][RX], const float* tile, const float* kplane, int ry, int ky)
+{
+	const int rows = RY + 2 * ry;
+	if constexpr (RX == kRX) {
+#pragma unroll 1
+		for (int r = 0; r < rows; ++r) row_sums<KX, P, RX, RY, true>(sum, tile, kplane, ry, ky, r);
+	} else {
+		// rows RY - 1 .. 2 ry feed all RY output rows; the first and last RY - 1 rows feed some
+		const int lo = RY - 1 < 2 * ry + 1 ? RY - 1 : 2 * ry + 1;
+		const int hi = 2 * ry + 1 > lo ? 2 * ry + 1 : lo;
+#pragma unroll 1
+		for (int r = 0; r < lo; ++r) row_sums<KX, P, RX, RY, true>(sum, tile, kplane, ry, ky, r);
+#pragma unroll 1
+		for (int r = lo; r < hi; ++r) row_sums<KX, P, RX, RY, false>(sum, tile, kplane, ry, ky, r);
+#pragma unroll 1
+		for (int r = hi; r < rows; ++r) row_sums<KX, P, RX, RY, true>(sum, tile, kplane, ry, ky, r);
 	}
 }
 
@@ -261,10 +287,12 @@ __device__ __forceinline__ void plane_sums(float (&sum)[kRY][kRX], const float* 
 // (bit b for buffer b) from one call to the next, and `bars` are the two tile mbarriers (TMA
 // stages), initialised by the caller. The caller applies its epilogue to acc afterwards, so
 // none of the epilogue's state is live during the sums.
-template<int KX, int WX, int WY, int STAGE, bool SINGLE = false>
+template<int KX, int WX, int WY, int STAGE, bool SINGLE = false, int RX = kRX, int RY = kRY>
 __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, const TileArgs& a, int x0, int y0, int z,
-	uint32_t& phases, uint64_t* bars, float (&acc)[kRY][kRX])
+	uint32_t& phases, uint64_t* bars, float (&acc)[RY][RX])
 {
+	static_assert(RX % 4 == 0 && RX * RY == kRX * kRY && 32 % RX == 0, "a lane owns 32 outputs of a 32 x 32 warp tile");
+	constexpr int LX = 32 / RX; // lanes along x in a warp
 	using G = TileGeom<KX>;
 	constexpr int TX = 32 * WX;
 	constexpr int TY = 32 * WY;
@@ -288,8 +316,8 @@ __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, cons
 	const int esize = (a.src_dtype == IANE_GB_U8 || a.src_dtype == IANE_GB_I8) ? 1 : 2;
 	const int narrow_pitch = narrow_box_elems<KX, WX>(esize) * esize;
 	const int narrow_buf = static_cast<int>(narrow_stage_bytes<KX, WX, WY>(ky, esize));
-	const int tx_b = (warp % WX) * 4 + (lane & 3);
-	const int ty_b = (warp / WX) * 8 + (lane >> 2);
+	const int tx_b = (warp % WX) * LX + (lane % LX);
+	const int ty_b = (warp / WX) * (32 / LX) + (lane / LX);
 	// a warp whose 32 x 32 outputs all lie outside the image (the ragged last tiles) skips the
 	// sums: the epilogue stores nothing there, so no result changes
 	const bool warp_active = x0 + 32 * (warp % WX) < a.nx && y0 + 32 * (warp / WX) < a.ny;
@@ -363,9 +391,9 @@ __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, cons
 
 
 #pragma unroll
-	for (int j = 0; j < kRY; ++j)
+	for (int j = 0; j < RY; ++j)
 #pragma unroll
-		for (int i = 0; i < kRX; ++i) acc[j][i] = 0.0f;
+		for (int i = 0; i < RX; ++i) acc[j][i] = 0.0f;
 
 	bool ok = true;
 	// TMA with a clamp or mirror border: a tile that reaches outside the image gets its
@@ -415,23 +443,23 @@ __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, cons
 			}
 			__syncthreads();
 		}
-		const float* tile = tiles + (p & 1) * plane_floats + (kRY * ty_b) * P + kRX * tx_b;
+		const float* tile = tiles + (p & 1) * plane_floats + (RY * ty_b) * P + RX * tx_b;
 		const float* kplane = psf_s + (p & 1) * psf_floats;
 		if (!warp_active) {
 			// nothing to sum
 		} else if constexpr (SINGLE) {
-			plane_sums<KX, P>(acc, tile, kplane, ry, ky);
+			plane_sums<KX, P, RX, RY>(acc, tile, kplane, ry, ky);
 		} else {
-			float part[kRY][kRX];
+			float part[RY][RX];
 #pragma unroll
-			for (int j = 0; j < kRY; ++j)
+			for (int j = 0; j < RY; ++j)
 #pragma unroll
-				for (int i = 0; i < kRX; ++i) part[j][i] = 0.0f;
-			plane_sums<KX, P>(part, tile, kplane, ry, ky);
+				for (int i = 0; i < RX; ++i) part[j][i] = 0.0f;
+			plane_sums<KX, P, RX, RY>(part, tile, kplane, ry, ky);
 #pragma unroll
-			for (int j = 0; j < kRY; ++j)
+			for (int j = 0; j < RY; ++j)
 #pragma unroll
-				for (int i = 0; i < kRX; ++i) acc[j][i] += part[j][i];
+				for (int i = 0; i < RX; ++i) acc[j][i] += part[j][i];
 		}
 
 
@@ -443,13 +471,14 @@ __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, cons
 	}
 }
 
-// Origin of this thread's kRX x kRY outputs within the tile at (x0, y0) of a WX-warp-wide block.
-template<int WX>
+// Origin of this thread's RX x RY outputs within the tile at (x0, y0) of a WX-warp-wide block.
+template<int WX, int RX = kRX, int RY = kRY>
 __device__ __forceinline__ void tile_origin(int x0, int y0, int& xo, int& yo)
 {
+	constexpr int LX = 32 / RX;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	xo = x0 + kRX * ((warp % WX) * 4 + (lane & 3));
-	yo = y0 + kRY * ((warp / WX) * 8 + (lane >> 2));
+	xo = x0 + RX * ((warp % WX) * LX + (lane % LX));
+	yo = y0 + RY * ((warp / WX) * (32 / LX) + (lane / LX));
 }
 
 // Shared memory bytes of the tile barriers (after the tiles and taps of conv_tile_sums).

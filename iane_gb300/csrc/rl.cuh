@@ -32,24 +32,28 @@ struct EpiRatio {
 		return obs_u8 ? static_cast<float>(*reinterpret_cast<const uint8_t*>(p)) : *reinterpret_cast<const float*>(p);
 	}
 
-	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[kRX]) const
+	// N outputs of one row starting at xo (N a multiple of 4; xo a multiple of 4)
+	template<int N>
+	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[N]) const
 	{
 		if (y >= ny) {
 			return;
 		}
-		float r[kRX];
+		float r[N];
 #pragma unroll
-		for (int i = 0; i < kRX; ++i) {
+		for (int i = 0; i < N; ++i) {
 			const float p = v[i];
 			r[i] = xo + i < nx ? observed(xo + i, y, z) / (p > eps ? p : eps) : 0.0f;
 		}
 		float* out = ratio + z * plane + y * pitch + xo;
-		if (xo + kRX <= nx) {
-			reinterpret_cast<float4*>(out)[0] = make_float4(r[0], r[1], r[2], r[3]);
-			reinterpret_cast<float4*>(out)[1] = make_float4(r[4], r[5], r[6], r[7]);
+		if (xo + N <= nx) {
+#pragma unroll
+			for (int m = 0; m < N / 4; ++m) {
+				reinterpret_cast<float4*>(out)[m] = make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+			}
 		} else {
 #pragma unroll
-			for (int i = 0; i < kRX; ++i) {
+			for (int i = 0; i < N; ++i) {
 				if (xo + i < nx) out[i] = r[i];
 			}
 		}
@@ -98,29 +102,32 @@ struct EpiUpdate {
 	// per-thread Kahan state
 	float f_s, f_c, c_s, c_c, n_s, n_c;
 
-	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[kRX])
+	// N outputs of one row starting at xo (N a multiple of 4; xo a multiple of 4)
+	template<int N>
+	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[N])
 	{
 		if (y >= ny) {
 			return;
 		}
-		const bool interior = xo >= ilo[0] && xo + kRX - 1 <= ihi[0] && y >= ilo[1] && y <= ihi[1] &&
+		const bool interior = xo >= ilo[0] && xo + N - 1 <= ihi[0] && y >= ilo[1] && y <= ihi[1] &&
 			z >= ilo[2] && z <= ihi[2];
 		float* e = est + z * plane + y * pitch + xo;
-		float old[kRX];
-		const bool full = xo + kRX <= nx;
+		float old[N];
+		const bool full = xo + N <= nx;
 		if (full) {
-			const float4 a = reinterpret_cast<const float4*>(e)[0];
-			const float4 b = reinterpret_cast<const float4*>(e)[1];
-			old[0] = a.x; old[1] = a.y; old[2] = a.z; old[3] = a.w;
-			old[4] = b.x; old[5] = b.y; old[6] = b.z; old[7] = b.w;
+#pragma unroll
+			for (int m = 0; m < N / 4; ++m) {
+				const float4 a = reinterpret_cast<const float4*>(e)[m];
+				old[4 * m] = a.x; old[4 * m + 1] = a.y; old[4 * m + 2] = a.z; old[4 * m + 3] = a.w;
+			}
 		} else {
 #pragma unroll
-			for (int i = 0; i < kRX; ++i) old[i] = xo + i < nx ? e[i] : 0.0f;
+			for (int i = 0; i < N; ++i) old[i] = xo + i < nx ? e[i] : 0.0f;
 		}
-		float upd[kRX];
+		float upd[N];
 		const int cyz = interior ? 0 : cx_count * (cls[nx + y] + cy_count * cls[nx + ny + z]);
 #pragma unroll
-		for (int i = 0; i < kRX; ++i) {
+		for (int i = 0; i < N; ++i) {
 			float s = s_interior;
 			if (!interior && xo + i < nx) {
 				s = sens[cls[xo + i] + cyz];
@@ -129,16 +136,18 @@ struct EpiUpdate {
 			upd[i] = old[i] * factor;
 		}
 		if (full) {
-			reinterpret_cast<float4*>(e)[0] = make_float4(upd[0], upd[1], upd[2], upd[3]);
-			reinterpret_cast<float4*>(e)[1] = make_float4(upd[4], upd[5], upd[6], upd[7]);
+#pragma unroll
+			for (int m = 0; m < N / 4; ++m) {
+				reinterpret_cast<float4*>(e)[m] = make_float4(upd[4 * m], upd[4 * m + 1], upd[4 * m + 2], upd[4 * m + 3]);
+			}
 		} else {
 #pragma unroll
-			for (int i = 0; i < kRX; ++i) {
+			for (int i = 0; i < N; ++i) {
 				if (xo + i < nx) e[i] = upd[i];
 			}
 		}
 #pragma unroll
-		for (int i = 0; i < kRX; ++i) {
+		for (int i = 0; i < N; ++i) {
 			if (xo + i < nx) {
 				if (want_stats) {
 					kahan_add(f_s, f_c, upd[i]);

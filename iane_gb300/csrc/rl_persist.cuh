@@ -70,6 +70,10 @@ __device__ __forceinline__ bool wait_counter(const unsigned int* word, unsigned 
 	return false;
 }
 
+// Lane geometry of the persistent kernel's tile body: 16 x by 2 y outputs per lane (conv_tile.cuh).
+constexpr int kPersistRX = 16;
+constexpr int kPersistRY = 2;
+
 // Shared memory of the persistent kernel: the tiled body's tiles, taps and barriers, then the
 // item index.
 template<int KX>
@@ -129,21 +133,21 @@ __global__ void __launch_bounds__(128, 4) rl_persist_kernel(const __grid_constan
 		const int x0 = (tile % p.tiles_x) * 64;
 		const int y0 = (tile / p.tiles_x) * 64;
 		const bool pass_b = phase & 1;
-		float acc[kRY][kRX];
-		conv_tile_sums<KX, 2, 2, kTileTma, false>(pass_b ? &p.map_ratio : &p.map_est, pass_b ? p.pass_b : p.pass_a,
-			x0, y0, z, tile_phases, bars, acc);
+		float acc[kPersistRY][kPersistRX];
+		conv_tile_sums<KX, 2, 2, kTileTma, false, kPersistRX, kPersistRY>(pass_b ? &p.map_ratio : &p.map_est,
+			pass_b ? p.pass_b : p.pass_a, x0, y0, z, tile_phases, bars, acc);
 		int xo = 0, yo = 0;
-		tile_origin<2>(x0, y0, xo, yo);
+		tile_origin<2, kPersistRX, kPersistRY>(x0, y0, xo, yo);
 		if (pass_b) {
 			EpiUpdate epi = p.epi_b; // read only after the sums: not live during them
 			epi.want_stats = 0;
 			epi.write_out = phase == p.phases - 1 ? p.epi_b.write_out : 0;
 #pragma unroll
-			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, z, acc[j]);
+			for (int j = 0; j < kPersistRY; ++j) epi.row(xo, yo + j, z, acc[j]);
 		} else {
 			const EpiRatio epi = p.epi_a;
 #pragma unroll
-			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, z, acc[j]);
+			for (int j = 0; j < kPersistRY; ++j) epi.row(xo, yo + j, z, acc[j]);
 		}
 		fence_proxy_async_global(); // this thread's epilogue stores, before other items' TMA reads
 		__syncthreads();
