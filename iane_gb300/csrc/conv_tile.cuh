@@ -493,7 +493,7 @@ __device__ __forceinline__ uint64_t* tile_barriers(int ky, int kz)
 		tile_buffers(kz) * (plane_floats + psf_floats));
 }
 
-template<int KX, int WX, int WY, int STAGE, class Epi, bool SINGLE>
+template<int KX, int WX, int WY, int STAGE, class Epi, bool SINGLE, int RX, int RY>
 __global__ void __launch_bounds__(32 * WX * WY)
 	conv_tile_kernel(const __grid_constant__ CUtensorMap tmap, const TileArgs a, const __grid_constant__ Epi epi_in)
 {
@@ -507,25 +507,25 @@ __global__ void __launch_bounds__(32 * WX * WY)
 	}
 	uint32_t phases = 0;
 	const int x0 = blockIdx.x * 32 * WX, y0 = blockIdx.y * 32 * WY;
-	float acc[kRY][kRX];
-	conv_tile_sums<KX, WX, WY, STAGE, SINGLE>(&tmap, a, x0, y0, blockIdx.z, phases, tile_barriers<KX, WX, WY>(a.ky, a.kz),
-		acc);
+	float acc[RY][RX];
+	conv_tile_sums<KX, WX, WY, STAGE, SINGLE, RX, RY>(&tmap, a, x0, y0, blockIdx.z, phases,
+		tile_barriers<KX, WX, WY>(a.ky, a.kz), acc);
 	// the epilogue's state (pointers, Kahan sums) comes to life only after the sums
 	Epi epi = epi_in;
 	int xo = 0, yo = 0;
-	tile_origin<WX>(x0, y0, xo, yo);
+	tile_origin<WX, RX, RY>(x0, y0, xo, yo);
 #pragma unroll
-	for (int j = 0; j < kRY; ++j) {
+	for (int j = 0; j < RY; ++j) {
 		epi.row(xo, yo + j, blockIdx.z, acc[j]);
 	}
 	epi.finish();
 }
 
-// Launch helper: grid = tiles over (x, y) and one block per output plane.
-template<int KX, int WX, int WY, int STAGE, bool SINGLE = false, class Epi>
+// Launch helper: grid = tiles over (x, y) and one block per output plane; RX x RY outputs per lane.
+template<int KX, int WX, int WY, int STAGE, bool SINGLE = false, int RX = kRX, int RY = kRY, class Epi>
 int launch_tile(const CUtensorMap& map, const TileArgs& a, const Epi& epi, cudaStream_t stream)
 {
-	auto kernel = conv_tile_kernel<KX, WX, WY, STAGE, Epi, SINGLE>;
+	auto kernel = conv_tile_kernel<KX, WX, WY, STAGE, Epi, SINGLE, RX, RY>;
 	const int esize = (a.src_dtype == IANE_GB_U8 || a.src_dtype == IANE_GB_I8) ? 1 : 2;
 	const size_t smem = tile_smem_bytes<KX, WX, WY>(a.ky, a.kz, STAGE, esize);
 	IANE_GB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
@@ -545,37 +545,44 @@ struct EpiStoreF32 {
 	int vec4;   // rows start 16-byte aligned and axis 0 is packed
 	int dtype;  // destination element type (0 or IANE_GB_F32: f32)
 
-	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[kRX]) const
+	// N outputs of one row starting at xo (N 8 or 16; xo a multiple of N)
+	template<int N>
+	__device__ __forceinline__ void row(int xo, int y, int z, const float (&v)[N]) const
 	{
+		static_assert(N == 8 || N == 16, "8 or 16 outputs per lane row");
 		if (y >= ny) {
 			return;
 		}
 		char* base = dst + y * stride[1] + z * stride[2];
 		if (dtype != 0 && dtype != IANE_GB_F32) {
-			if (dtype == IANE_GB_U8 && vec4 && xo + kRX <= nx) {
-				// packed rows: the lane's 8 bytes in one 8-byte store
-				uint32_t w[2] = {0u, 0u};
+			if (dtype == IANE_GB_U8 && vec4 && xo + N <= nx) {
+				// packed rows: the lane's N bytes in one N-byte store
+				uint32_t w[N / 4] = {};
 #pragma unroll
-				for (int i = 0; i < kRX; ++i) w[i >> 2] |= static_cast<uint32_t>(convert_f32_u8(v[i])) << (8 * (i & 3));
-				*reinterpret_cast<uint2*>(base + xo) = make_uint2(w[0], w[1]);
+				for (int i = 0; i < N; ++i) w[i >> 2] |= static_cast<uint32_t>(convert_f32_u8(v[i])) << (8 * (i & 3));
+				if constexpr (N == 8) {
+					*reinterpret_cast<uint2*>(base + xo) = make_uint2(w[0], w[1]);
+				} else {
+					*reinterpret_cast<uint4*>(base + xo) = make_uint4(w[0], w[1], w[2], w[3]);
+				}
 				return;
 			}
 #pragma unroll
-			for (int i = 0; i < kRX; ++i) {
+			for (int i = 0; i < N; ++i) {
 				if (xo + i < nx) {
 					store_converted_f32(base + (xo + i) * stride[0], dtype, v[i]);
 				}
 			}
 			return;
 		}
-		if (vec4 && xo + kRX <= nx) {
+		if (vec4 && xo + N <= nx) {
 			float4* p = reinterpret_cast<float4*>(base + xo * 4LL);
-			p[0] = make_float4(v[0], v[1], v[2], v[3]);
-			p[1] = make_float4(v[4], v[5], v[6], v[7]);
+#pragma unroll
+			for (int m = 0; m < N / 4; ++m) p[m] = make_float4(v[4 * m], v[4 * m + 1], v[4 * m + 2], v[4 * m + 3]);
 			return;
 		}
 #pragma unroll
-		for (int i = 0; i < kRX; ++i) {
+		for (int i = 0; i < N; ++i) {
 			if (xo + i < nx) {
 				*reinterpret_cast<float*>(base + (xo + i) * stride[0]) = v[i];
 			}
