@@ -37,12 +37,11 @@ __device__ bool wait_for_image(const BatchSync& sync, int image, unsigned int ne
 }
 
 // The sums of one item's tile for its PSF width (the epilogue is applied by the caller).
-template<bool PASS_B>
-__device__ __forceinline__ void item_sums(const BatchImage& im, int x0, int y0, uint32_t& phases, uint64_t* bars,
-	float (&acc)[kRY][kRX])
+__device__ __forceinline__ void item_sums(const BatchImage& im, bool pass_b, int x0, int y0, uint32_t& phases,
+	uint64_t* bars, float (&acc)[kRY][kRX])
 {
-	const CUtensorMap* map = PASS_B ? &im.map_ratio : &im.map_est;
-	const TileArgs& a = PASS_B ? im.pass_b : im.pass_a;
+	const CUtensorMap* map = pass_b ? &im.map_ratio : &im.map_est;
+	const TileArgs& a = pass_b ? im.pass_b : im.pass_a;
 #define IANE_GB_BATCH_KX(K) \
 	case K: conv_tile_sums<K, 2, 2, kTileTma, true>(map, a, x0, y0, 0, phases, bars, acc); break;
 	switch (im.kx) {
@@ -98,15 +97,14 @@ __global__ void __launch_bounds__(128) batch_persistent_kernel(const BatchImage*
 		float acc[kRY][kRX];
 		int xo = 0, yo = 0;
 		tile_origin<2>(x0, y0, xo, yo);
+		item_sums(im, phase & 1, x0, y0, tile_phases, bars, acc);
 		if (phase & 1) {
-			item_sums<true>(im, x0, y0, tile_phases, bars, acc);
 			EpiUpdate epi = im.epi_b; // read only after the sums: not live during them
 			epi.want_stats = 0;
 			epi.write_out = phase == phases - 1 && im.write_out_final;
 #pragma unroll
 			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
 		} else {
-			item_sums<false>(im, x0, y0, tile_phases, bars, acc);
 			const EpiRatio epi = im.epi_a;
 #pragma unroll
 			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
