@@ -332,6 +332,31 @@ __device__ __forceinline__ void fence_proxy_async_global()
 	asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
+// Bounded wait until *word >= need. False if the run was aborted or the wait gave up (which it
+// records in the status word and turns into an abort).
+__device__ __forceinline__ bool wait_counter(const unsigned int* word, unsigned int need, int* abort, int* status)
+{
+	if (load_acquire(word) >= need) {
+		return true;
+	}
+	const uint64_t t0 = global_ns();
+	for (uint32_t i = 1; i < (1u << 26); ++i) {
+		if (load_acquire(word) >= need) {
+			return true;
+		}
+		if (load_volatile(abort)) {
+			return false;
+		}
+		if ((i & 63u) == 0 && global_ns() - t0 > 2000000000ull) {
+			break;
+		}
+		__nanosleep(64);
+	}
+	report_device_status(status, IANE_GB_DEVICE_TIMEOUT);
+	atomicExch(abort, 1);
+	return false;
+}
+
 // Bounded wait on an mbarrier phase: gives up (returns false) after `limit_ns` of global time
 // -- two seconds unless told otherwise -- or 2^26 tries, whichever comes first, so that a
 // phase that never completes ends the kernel instead of hanging it. The caller records the

@@ -9,32 +9,6 @@ namespace {
 
 // Bytes after the tiles and taps: the two tile mbarriers and the item index.
 constexpr size_t kBatchTail = 32;
-constexpr uint64_t kWaitLimitNs = 2000000000ull;
-
-// Thread 0: wait until image `image` has completed `need` tiles. False if the run is aborted or
-// the wait gave up (which it records and turns into an abort).
-__device__ bool wait_for_image(const BatchSync& sync, int image, unsigned int need, int* status)
-{
-	if (load_acquire(&sync.done[image]) >= need) {
-		return true;
-	}
-	const uint64_t t0 = global_ns();
-	for (uint32_t i = 1; i < (1u << 26); ++i) {
-		if (load_acquire(&sync.done[image]) >= need) {
-			return true;
-		}
-		if (load_volatile(sync.abort)) {
-			return false;
-		}
-		if ((i & 63u) == 0 && global_ns() - t0 > kWaitLimitNs) {
-			break;
-		}
-		__nanosleep(128);
-	}
-	report_device_status(status, IANE_GB_DEVICE_TIMEOUT);
-	atomicExch(sync.abort, 1);
-	return false;
-}
 
 // The sums of one item's tile for its PSF width (the epilogue is applied by the caller).
 __device__ __forceinline__ void item_sums(const BatchImage& im, bool pass_b, int x0, int y0, uint32_t& phases,
@@ -78,7 +52,9 @@ __global__ void __launch_bounds__(128) batch_persistent_kernel(const BatchImage*
 				const int phase = static_cast<int>(k / static_cast<unsigned int>(items_per_phase));
 				const BatchItem w = items[k - static_cast<unsigned int>(phase) * items_per_phase];
 				if (phase > 0) {
-					go = wait_for_image(sync, w.image, static_cast<unsigned int>(phase) * images[w.image].tiles, status);
+					// the image's previous phase complete (bounded: a wait that gives up aborts the run)
+					go = wait_counter(&sync.done[w.image], static_cast<unsigned int>(phase) * images[w.image].tiles,
+						sync.abort, status);
 					fence_proxy_async_global(); // the image's previous phase, written by generic stores, before TMA
 				}
 			}

@@ -45,31 +45,6 @@ int launch_rl_persist(int kx, const RlPersistArgs& p, cudaStream_t stream);
 int launch_rl_persist_lo(int kx, const RlPersistArgs& p, cudaStream_t stream);
 int launch_rl_persist_hi(int kx, const RlPersistArgs& p, cudaStream_t stream);
 
-// Bounded wait until *word >= need. False if the run was aborted or the wait gave up (which it
-// records in the status word and turns into an abort).
-__device__ __forceinline__ bool wait_counter(const unsigned int* word, unsigned int need, int* abort, int* status)
-{
-	if (load_acquire(word) >= need) {
-		return true;
-	}
-	const uint64_t t0 = global_ns();
-	for (uint32_t i = 1; i < (1u << 26); ++i) {
-		if (load_acquire(word) >= need) {
-			return true;
-		}
-		if (load_volatile(abort)) {
-			return false;
-		}
-		if ((i & 63u) == 0 && global_ns() - t0 > 2000000000ull) {
-			break;
-		}
-		__nanosleep(64);
-	}
-	report_device_status(status, IANE_GB_DEVICE_TIMEOUT);
-	atomicExch(abort, 1);
-	return false;
-}
-
 // Lane geometry of the persistent kernel's tile body: 16 x by 2 y outputs per lane (conv_tile.cuh).
 constexpr int kPersistRX = 16;
 constexpr int kPersistRY = 2;
