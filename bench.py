@@ -495,7 +495,8 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
     ms = a.elapsed_time(b) / reps
     pixels = sum(o.numel() for o in obs)
     macs = sum(o.numel() * p.size for o, p in zip(obs, psfs)) * 2 * iterations
-    bps, order = batch.launch_config()
+    bps, order, grouping = batch.launch_config()
+    widths = batch.tile_widths()
     batch.close()
     assert all(bool(torch.isfinite(o).all()) for o in outs)
     peaks, _ = measured_peaks()
@@ -506,7 +507,8 @@ def measure_batch_leg(dev, stream, reps=3, iterations=30, cpu=True):
            "gvoxel_s": 2 * iterations * pixels / (ms / 1e3) / 1e9, "tflops_useful": 2 * macs / (ms / 1e3) / 1e12,
            "gbs_algorithmic": alg_bytes / (ms / 1e3) / 1e9,
            "launch": {"persistent_launches_per_run": 1, "ctas_per_sm": bps,
-                      "queue_order": ["largest images first", "by PSF width"][order], "tile": "64x64"},
+                      "queue_order": ["largest images first", "by PSF width"][order], "grouping": grouping,
+                      "images_by_item_shape": {f"{w}x64": widths.count(w) for w in sorted(set(widths))}},
            "prepare_s": prepare_s}
     res["frac_of_fp32_peak"] = res["tflops_useful"] / fp32
     res["frac_of_hbm_peak"] = res["gbs_algorithmic"] / hbm

@@ -387,11 +387,17 @@ class RichardsonLucyBatch:
         return list(out)
 
     def launch_config(self):
-        """(CTAs per SM, queue order) of the persistent launch: 0 = largest images first,
-        1 = grouped by PSF width."""
-        bps, order = ctypes.c_int32(0), ctypes.c_int32(0)
-        check(lib().iane_gb_rl_batch_config(self._batch, ctypes.byref(bps), ctypes.byref(order)))
-        return int(bps.value), int(order.value)
+        """(CTAs per SM, queue order, grouping) of the persistent launch: order 0 = largest
+        images first, 1 = grouped by PSF width; grouping 0-3 = the work items' shapes (tiles per
+        item by PSF width, see ``tile_widths``)."""
+        bps, order, group = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+        check(lib().iane_gb_rl_batch_config(self._batch, ctypes.byref(bps), ctypes.byref(order),
+                                            ctypes.byref(group)))
+        return int(bps.value), int(order.value), int(group.value)
+
+    def configure(self, blocks_per_sm: int, order: int, grouping: int) -> None:
+        """Pin the launch configuration (same results for any configuration)."""
+        check(lib().iane_gb_rl_batch_configure(self._batch, int(blocks_per_sm), int(order), int(grouping)))
 
     def run(self, observed, estimates, iterations: int, epsilon: float = 1e-6, init: int = abi.RL_INIT_OBSERVED,
             scratch=None, stream=None):

@@ -85,8 +85,10 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_rl_batch_scratch_bytes.restype = ctypes.c_size_t
     l.iane_gb_rl_batch_tiles.argtypes = [cvp, i32p]
     l.iane_gb_rl_batch_tiles.restype = ctypes.c_int
-    l.iane_gb_rl_batch_config.argtypes = [cvp, i32p, i32p]
+    l.iane_gb_rl_batch_config.argtypes = [cvp, i32p, i32p, i32p]
     l.iane_gb_rl_batch_config.restype = ctypes.c_int
+    l.iane_gb_rl_batch_configure.argtypes = [cvp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    l.iane_gb_rl_batch_configure.restype = ctypes.c_int
     l.iane_gb_rl_batch_run.argtypes = [vp, _VIEW_P, _VIEW_P, ctypes.c_int, ctypes.c_float, ctypes.c_int, vp,
                                        ctypes.c_size_t, vp]
     l.iane_gb_rl_batch_run.restype = ctypes.c_int

@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import ctypes
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_RANK = 3
 
 U8, U16, I16, I32, F32, F64, BF16, I8, U32, RGB8 = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10

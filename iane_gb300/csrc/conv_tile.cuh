@@ -287,9 +287,10 @@ __device__ __forceinline__ void plane_sums(float (&sum)[RY][RX], const float* ti
 // (bit b for buffer b) from one call to the next, and `bars` are the two tile mbarriers (TMA
 // stages), initialised by the caller. The caller applies its epilogue to acc afterwards, so
 // none of the epilogue's state is live during the sums.
+// taps_resident: a single-plane caller's previous call left this kernel's taps in shared memory.
 template<int KX, int WX, int WY, int STAGE, bool SINGLE = false, int RX = kRX, int RY = kRY>
 __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, const TileArgs& a, int x0, int y0, int z,
-	uint32_t& phases, uint64_t* bars, float (&acc)[RY][RX])
+	uint32_t& phases, uint64_t* bars, float (&acc)[RY][RX], bool taps_resident = false)
 {
 	static_assert(RX % 4 == 0 && RX * RY == kRX * kRY && 32 % RX == 0, "a lane owns 32 outputs of a 32 x 32 warp tile");
 	constexpr int LX = 32 / RX; // lanes along x in a warp
@@ -345,7 +346,7 @@ __device__ __forceinline__ void conv_tile_sums(const CUtensorMap* tmap_ptr, cons
 			dst[i] = v;
 		}
 	};
-	if (nplanes > 0) load_taps(0);
+	if (nplanes > 0 && !(SINGLE && taps_resident)) load_taps(0);
 	if (nplanes > 1) load_taps(1);
 	__syncthreads(); // taps visible; every lane is done with the previous tile's buffers
 

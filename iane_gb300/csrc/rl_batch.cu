@@ -5,6 +5,7 @@
 #include "rl_batch.cuh"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -101,8 +102,22 @@ constexpr int kOrderLargestFirst = 0; // images by descending tile count
 constexpr int kOrderByWidth = 1;      // images by PSF width, then by descending tile count
 constexpr int kOrders = 2;
 
+// Item shapes: tiles per item (along x) by PSF width, one rule per grouping level. Narrow PSFs
+// do little arithmetic per tile, so their items carry the per-item queue, dependency and
+// completion work over several tiles and load the taps once.
+constexpr int kGroups = 4;
+int tiles_per_item(int kx, int group)
+{
+	switch (group) {
+	case 1: return kx <= 11 ? 2 : 1;
+	case 2: return kx <= 11 ? 4 : 1;
+	case 3: return kx <= 7 ? 4 : (kx <= 15 ? 2 : 1);
+	default: return 1;
+	}
+}
+
 std::vector<BatchItem> make_items(const std::vector<int>& nx, const std::vector<int>& ny, const std::vector<int>& kx,
-	int order)
+	int order, int group)
 {
 	const int n = static_cast<int>(nx.size());
 	std::vector<int> idx(n);
@@ -114,19 +129,22 @@ std::vector<BatchItem> make_items(const std::vector<int>& nx, const std::vector<
 	});
 	std::vector<BatchItem> items;
 	for (int i : idx) {
-		for (int t = 0; t < tiles(i); ++t) items.push_back(BatchItem{i, t});
+		const int tx = tiles_of(nx[i]), ty = tiles_of(ny[i]), s = tiles_per_item(kx[i], group);
+		for (int r = 0; r < ty; ++r) {
+			for (int c = 0; c < tx; c += s) items.push_back(BatchItem{i, r * tx + c, std::min(s, tx - c)});
+		}
 	}
 	return items;
 }
 
 // ---------------------------------------------------------------------------------------
-// autotuner: CTAs per SM and queue order per batch (shapes, PSF sizes, dtype, SM count),
-// cached in a text file
+// autotuner: CTAs per SM, queue order and item shapes per batch (shapes, PSF sizes, dtype,
+// SM count), cached in a text file
 
 struct TuneCache {
 	std::mutex lock;
 	bool loaded = false;
-	std::map<std::string, std::pair<int, int>> choice; // key -> (CTAs per SM, order)
+	std::map<std::string, std::array<int, 3>> choice; // key -> (CTAs per SM, order, grouping)
 	std::string path;
 };
 
@@ -174,14 +192,15 @@ void load_cache(TuneCache& c)
 	std::ifstream in(c.path);
 	std::string line;
 	while (std::getline(in, line)) {
-		// "<key> | <ms per configuration ...> | <CTAs per SM> <order>"
+		// "<key> | <ms per configuration ...> | <CTAs per SM> <order> <grouping>"
 		const auto first = line.find(" | ");
 		const auto last = line.rfind(" | ");
 		if (first == std::string::npos || last == first) continue;
 		std::istringstream tail(line.substr(last + 3));
-		int bps = 0, order = -1;
+		int bps = 0, order = -1, group = 0;
 		if (tail >> bps >> order && bps > 0 && order >= 0 && order < kOrders) {
-			c.choice[line.substr(0, first)] = {bps, order};
+			if (!(tail >> group) || group < 0 || group >= kGroups) group = 0;
+			c.choice[line.substr(0, first)] = {bps, order, group};
 		}
 	}
 }
@@ -201,6 +220,7 @@ struct iane_gb_rl_batch {
 	size_t smem = 0;                       // dynamic shared memory of the launch
 	int blocks_per_sm = 1;                 // resident CTAs per SM the launch uses
 	int order = 0;                         // queue order (autotuned)
+	int group = 0;                         // item shapes by PSF width (autotuned, tiles_per_item)
 	iane_gb::BatchImage* d_images = nullptr;
 	iane_gb::InitDesc* d_init = nullptr;
 	size_t parts_off = 0, sync_off = 0, scratch_bytes = 0;
@@ -337,8 +357,9 @@ int autotune(iane_gb_rl_batch* b, cudaStream_t stream)
 	const auto hit = cache.choice.find(key);
 	const int max_bps = batch_blocks_per_sm(b->smem);
 	if (hit != cache.choice.end()) {
-		b->blocks_per_sm = std::min(hit->second.first, max_bps);
-		b->order = hit->second.second;
+		b->blocks_per_sm = std::min(hit->second[0], max_bps);
+		b->order = hit->second[1];
+		b->group = hit->second[2];
 		return IANE_GB_OK;
 	}
 	int* status = device_status_ptr();
@@ -398,31 +419,39 @@ int autotune(iane_gb_rl_batch* b, cudaStream_t stream)
 		return release(cuda_fail(cudaGetLastError(), "autotune: upload"));
 	}
 	const BatchSync sync = sync_words(b, base);
-	const int T = static_cast<int>(b->items.size());
 	const int sms = device_sm_count();
 	std::ostringstream timings;
 	float best = 0.0f;
-	for (int order = 0; order < kOrders; ++order) {
-		const std::vector<BatchItem> items = make_items(b->nx, b->ny, b->kx, order);
+	// ms of a two-iteration run of the whole batch with one launch configuration
+	auto time_config = [&](int order, int group, int bps, float& ms) -> int {
+		const std::vector<BatchItem> items = make_items(b->nx, b->ny, b->kx, order, group);
 		if (cudaMemcpy(d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) != cudaSuccess) {
-			return release(cuda_fail(cudaGetLastError(), "autotune: upload items"));
+			return cuda_fail(cudaGetLastError(), "autotune: upload items");
 		}
+		ms = 0.0f;
+		for (int rep = 0; rep < 3; ++rep) {
+			if (cudaMemsetAsync(sync.queue, 0, sync_bytes(n), stream) != cudaSuccess) {
+				return cuda_fail(cudaGetLastError(), "autotune: clear queue");
+			}
+			cudaEventRecord(t0, stream);
+			const int s = launch_batch_persistent(d_images, d_items, static_cast<int>(items.size()), 4, sync, status,
+				bps * sms, b->smem, stream);
+			if (s) return s;
+			cudaEventRecord(t1, stream);
+			IANE_GB_CUDA(cudaEventSynchronize(t1), "autotune: time");
+			float e = 0.0f;
+			cudaEventElapsedTime(&e, t0, t1);
+			if (rep > 0) ms += e / 2.0f; // the first run warms up
+		}
+		timings << ms << ' ';
+		return IANE_GB_OK;
+	};
+	// CTAs per SM x queue order with one tile per item, then the item shapes at the best of those
+	for (int order = 0; order < kOrders; ++order) {
 		for (int bps = 1; bps <= max_bps; ++bps) {
 			float ms = 0.0f;
-			for (int rep = 0; rep < 3; ++rep) {
-				if (cudaMemsetAsync(sync.queue, 0, sync_bytes(n), stream) != cudaSuccess) {
-					return release(cuda_fail(cudaGetLastError(), "autotune: clear queue"));
-				}
-				cudaEventRecord(t0, stream);
-				st = launch_batch_persistent(d_images, d_items, T, 4, sync, status, bps * sms, b->smem, stream);
-				if (st) return release(st);
-				cudaEventRecord(t1, stream);
-				IANE_GB_CUDA(cudaEventSynchronize(t1), "autotune: time");
-				float e = 0.0f;
-				cudaEventElapsedTime(&e, t0, t1);
-				if (rep > 0) ms += e / 2.0f; // the first run warms up
-			}
-			timings << ms << ' ';
+			st = time_config(order, 0, bps, ms);
+			if (st) return release(st);
 			if (best == 0.0f || ms < best) {
 				best = ms;
 				b->blocks_per_sm = bps;
@@ -430,9 +459,21 @@ int autotune(iane_gb_rl_batch* b, cudaStream_t stream)
 			}
 		}
 	}
-	cache.choice[key] = {b->blocks_per_sm, b->order};
+	b->group = 0;
+	for (int group = 1; group < kGroups; ++group) {
+		float ms = 0.0f;
+		st = time_config(b->order, group, b->blocks_per_sm, ms);
+		if (st) return release(st);
+		if (ms < best) {
+			best = ms;
+			b->group = group;
+		}
+	}
+	cache.choice[key] = {b->blocks_per_sm, b->order, b->group};
 	std::ofstream log(cache.path, std::ios::app);
-	if (log) log << key << " | " << timings.str() << "| " << b->blocks_per_sm << ' ' << b->order << "\n";
+	if (log) {
+		log << key << " | " << timings.str() << "| " << b->blocks_per_sm << ' ' << b->order << ' ' << b->group << "\n";
+	}
 	return release(IANE_GB_OK);
 }
 
@@ -502,7 +543,8 @@ int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t*
 	b->scratch_bytes = off + kAlignB;
 	b->blocks_per_sm = batch_blocks_per_sm(b->smem);
 	b->order = kOrderLargestFirst;
-	b->items = make_items(b->nx, b->ny, b->kx, b->order);
+	b->group = 0;
+	b->items = make_items(b->nx, b->ny, b->kx, b->order, b->group);
 	if (cudaMalloc(&b->d_items, b->items.size() * sizeof(BatchItem)) != cudaSuccess ||
 	    cudaMalloc(&b->d_images, count * sizeof(BatchImage)) != cudaSuccess ||
 	    cudaMalloc(&b->d_init, count * sizeof(InitDesc)) != cudaSuccess ||
@@ -512,7 +554,7 @@ int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t*
 	if (flags & IANE_GB_BATCH_AUTOTUNE) {
 		const int st = autotune(b, static_cast<cudaStream_t>(stream));
 		if (st) return cleanup(st);
-		b->items = make_items(b->nx, b->ny, b->kx, b->order);
+		b->items = make_items(b->nx, b->ny, b->kx, b->order, b->group);
 	}
 	if (cudaMemcpy(b->d_items, b->items.data(), b->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) !=
 	    cudaSuccess) {
@@ -530,15 +572,39 @@ size_t iane_gb_rl_batch_scratch_bytes(const iane_gb_rl_batch* b)
 int iane_gb_rl_batch_tiles(const iane_gb_rl_batch* b, int32_t* tile_width)
 {
 	if (!b || !tile_width) return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_tiles: null argument");
-	for (int i = 0; i < b->count; ++i) tile_width[i] = kBatchTile;
+	for (int i = 0; i < b->count; ++i) tile_width[i] = kBatchTile * tiles_per_item(b->kx[i], b->group);
 	return IANE_GB_OK;
 }
 
-int iane_gb_rl_batch_config(const iane_gb_rl_batch* b, int32_t* blocks_per_sm, int32_t* order)
+int iane_gb_rl_batch_config(const iane_gb_rl_batch* b, int32_t* blocks_per_sm, int32_t* order, int32_t* grouping)
 {
-	if (!b || !blocks_per_sm || !order) return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_config: null argument");
+	if (!b || !blocks_per_sm || !order || !grouping) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_config: null argument");
+	}
 	*blocks_per_sm = b->blocks_per_sm;
 	*order = b->order;
+	*grouping = b->group;
+	return IANE_GB_OK;
+}
+
+int iane_gb_rl_batch_configure(iane_gb_rl_batch* b, int blocks_per_sm, int order, int grouping)
+{
+	if (!b) return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_configure: null batch");
+	if (blocks_per_sm < 1 || blocks_per_sm > batch_blocks_per_sm(b->smem) || order < 0 || order >= kOrders ||
+	    grouping < 0 || grouping >= kGroups) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "rl_batch_configure: configuration out of range");
+	}
+	std::vector<BatchItem> items = make_items(b->nx, b->ny, b->kx, order, grouping);
+	// a run still in flight may read the queue: wait for the device before replacing it (a
+	// grouping never makes more items than one tile per item, for which d_items was sized)
+	IANE_GB_CUDA(cudaDeviceSynchronize(), "rl_batch_configure: wait for running work");
+	IANE_GB_CUDA(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice),
+		"rl_batch_configure: upload work items");
+	b->items.swap(items);
+	b->blocks_per_sm = blocks_per_sm;
+	b->order = order;
+	b->group = grouping;
+	b->key.clear(); // the next run captures a graph with the new launch
 	return IANE_GB_OK;
 }
 

@@ -1,7 +1,7 @@
 // Batched Richardson-Lucy over many images of uneven size, each with its own PSF.
 //
 // The whole run -- every pass of every iteration of every image -- is ONE persistent launch
-// over a device work queue. The queue is the list of (image, 64x64 tile) items of one pass,
+// over a device work queue. The queue is the list of (image, run of 64x64 tiles) items of one pass,
 // repeated once per phase (phase 2t = pass A of iteration t, 2t + 1 = pass B); item k is
 // (phase k / T, entry k % T) for T items per pass. CTAs (a few per SM) take items from an
 // atomic counter in queue order and run the tiled FP32 convolution body with that image's TMA
@@ -39,13 +39,16 @@ struct alignas(64) BatchImage {
 	EpiUpdate epi_b;       // write_out is set only in the last iteration (write_out_final)
 	int kx;
 	int tiles_x;
-	int tiles;             // items of this image per phase
+	int tiles;             // 64x64 tiles of this image (completions per phase)
 	int write_out_final;
 };
 
+// `count` consecutive 64x64 tiles of one tile row of an image, from tile index `tile`: the
+// item's shape is (64 count) x 64 (count is 1, 2 or 4, chosen per PSF size by the autotuner).
 struct BatchItem {
 	int image;
 	int tile;
+	int count;
 };
 
 // Device words of a run, cleared before the launch: the queue counter, the abort flag and one

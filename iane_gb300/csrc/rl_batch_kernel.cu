@@ -12,12 +12,12 @@ constexpr size_t kBatchTail = 32;
 
 // The sums of one item's tile for its PSF width (the epilogue is applied by the caller).
 __device__ __forceinline__ void item_sums(const BatchImage& im, bool pass_b, int x0, int y0, uint32_t& phases,
-	uint64_t* bars, float (&acc)[kRY][kRX])
+	uint64_t* bars, float (&acc)[kRY][kRX], bool taps_resident)
 {
 	const CUtensorMap* map = pass_b ? &im.map_ratio : &im.map_est;
 	const TileArgs& a = pass_b ? im.pass_b : im.pass_a;
 #define IANE_GB_BATCH_KX(K) \
-	case K: conv_tile_sums<K, 2, 2, kTileTma, true>(map, a, x0, y0, 0, phases, bars, acc); break;
+	case K: conv_tile_sums<K, 2, 2, kTileTma, true>(map, a, x0, y0, 0, phases, bars, acc, taps_resident); break;
 	switch (im.kx) {
 	IANE_GB_BATCH_KX(1) IANE_GB_BATCH_KX(3) IANE_GB_BATCH_KX(5) IANE_GB_BATCH_KX(7)
 	IANE_GB_BATCH_KX(9) IANE_GB_BATCH_KX(11) IANE_GB_BATCH_KX(13) IANE_GB_BATCH_KX(15)
@@ -68,28 +68,32 @@ __global__ void __launch_bounds__(128) batch_persistent_kernel(const BatchImage*
 		const int phase = k / items_per_phase;
 		const BatchItem w = items[k - phase * items_per_phase];
 		const BatchImage& im = images[w.image];
-		const int x0 = (w.tile % im.tiles_x) * kBatchTile;
 		const int y0 = (w.tile / im.tiles_x) * kBatchTile;
-		float acc[kRY][kRX];
-		int xo = 0, yo = 0;
-		tile_origin<2>(x0, y0, xo, yo);
-		item_sums(im, phase & 1, x0, y0, tile_phases, bars, acc);
-		if (phase & 1) {
-			EpiUpdate epi = im.epi_b; // read only after the sums: not live during them
-			epi.want_stats = 0;
-			epi.write_out = phase == phases - 1 && im.write_out_final;
+		// the item's tiles, left to right along one tile row; the PSF taps stay in shared memory
+		// from the first tile to the last
+		for (int c = 0; c < w.count; ++c) {
+			const int x0 = (w.tile % im.tiles_x + c) * kBatchTile;
+			float acc[kRY][kRX];
+			int xo = 0, yo = 0;
+			tile_origin<2>(x0, y0, xo, yo);
+			item_sums(im, phase & 1, x0, y0, tile_phases, bars, acc, c > 0);
+			if (phase & 1) {
+				EpiUpdate epi = im.epi_b; // read only after the sums: not live during them
+				epi.want_stats = 0;
+				epi.write_out = phase == phases - 1 && im.write_out_final;
 #pragma unroll
-			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
-		} else {
-			const EpiRatio epi = im.epi_a;
+				for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
+			} else {
+				const EpiRatio epi = im.epi_a;
 #pragma unroll
-			for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
+				for (int j = 0; j < kRY; ++j) epi.row(xo, yo + j, 0, acc[j]);
+			}
 		}
 		fence_proxy_async_global(); // this thread's epilogue stores, before other tiles' TMA reads
 		__syncthreads();
 		if (threadIdx.x == 0) {
 			__threadfence();
-			atomicAdd(&sync.done[w.image], 1u);
+			atomicAdd(&sync.done[w.image], static_cast<unsigned int>(w.count));
 		}
 	}
 }

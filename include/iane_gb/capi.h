@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define IANE_GB_ABI_VERSION 1
+#define IANE_GB_ABI_VERSION 2
 #define IANE_GB_MAX_RANK 3
 
 /* Element types. */
@@ -299,11 +299,15 @@ int iane_gb_wiener_destroy(iane_gb_wiener_plan* plan);
  * queue of (image, 64x64 tile) items in pass order; an image's pass waits only until that
  * image's previous pass is complete (per-image completion counters, bounded waits), never for
  * the rest of the batch. The run is captured into a CUDA graph on the first call and replayed
- * while the views, scratch and parameters stay the same.
+ * while the views, scratch and parameters stay the same. A work item is a run of 1, 2 or 4
+ * consecutive tiles along x of one image (items of narrow PSFs carry the per-item queue,
+ * dependency and completion work over several tiles).
  * psfs: `count` f32 2-D device views (odd extents up to 31 x 63); extents: 2*count ints
- * (nx, ny per image). IANE_GB_BATCH_AUTOTUNE times the launch's CTAs per SM and its queue order
- * (largest images first, or grouped by PSF width) on this batch and caches the choice per
- * (image shapes, PSF sizes, dtype, SM count) in the file named by the environment variable
+ * (nx, ny per image). IANE_GB_BATCH_AUTOTUNE times the launch's CTAs per SM, its queue order
+ * (largest images first, or grouped by PSF width) and the work items' shapes (the grouping level:
+ * 0 one tile per item; 1 two tiles for PSFs up to 11 wide; 2 four tiles for PSFs up to 11 wide;
+ * 3 four tiles up to 7 wide and two up to 15) on this batch and caches the choice per (image
+ * shapes, PSF sizes, dtype, SM count) in the file named by the environment variable
  * IANE_GB_TUNE_CACHE (default $HOME/.cache/iane_gb300_tune.txt).
  */
 typedef struct iane_gb_rl_batch iane_gb_rl_batch;
@@ -312,10 +316,16 @@ typedef struct iane_gb_rl_batch iane_gb_rl_batch;
 int iane_gb_rl_batch_prepare(const iane_gb_view* psfs, int count, const int32_t* extents,
 	unsigned flags, void* stream, iane_gb_rl_batch** batch);
 size_t iane_gb_rl_batch_scratch_bytes(const iane_gb_rl_batch* batch);
-/* Tile width of every image's work items (64). */
+/* Width of every image's work items: 64 x the tiles per item (their height is 64). */
 int iane_gb_rl_batch_tiles(const iane_gb_rl_batch* batch, int32_t* tile_width);
-/* The persistent launch's CTAs per SM and queue order (0: largest images first, 1: by PSF width). */
-int iane_gb_rl_batch_config(const iane_gb_rl_batch* batch, int32_t* blocks_per_sm, int32_t* order);
+/* The persistent launch's CTAs per SM, queue order (0: largest images first, 1: by PSF width)
+ * and grouping level of the work items. */
+int iane_gb_rl_batch_config(const iane_gb_rl_batch* batch, int32_t* blocks_per_sm, int32_t* order,
+	int32_t* grouping);
+/* Pin the launch configuration (for example one tuned offline): CTAs per SM from 1 to the
+ * kernel's occupancy, order 0 or 1, grouping 0 to 3. The next run captures a new graph; results
+ * are the same bits whatever the configuration. */
+int iane_gb_rl_batch_configure(iane_gb_rl_batch* batch, int blocks_per_sm, int order, int grouping);
 /* observed / estimates: `count` views each (observed f32 or u8, estimate f32 or u8). */
 int iane_gb_rl_batch_run(iane_gb_rl_batch* batch, const iane_gb_view* observed,
 	const iane_gb_view* estimates, int iterations, float epsilon, int init, void* scratch,

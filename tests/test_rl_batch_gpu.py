@@ -139,8 +139,35 @@ def test_autotune_cache_persists(cuda, tmp_path):
     assert first.returncode == 0, first.stderr
     lines = cache.read_text().strip().splitlines()
     assert len(lines) == 1 and lines[0].count(" | ") == 2  # one measured line for the batch
-    assert "[64, 64, 64]" in first.stdout
+    widths = [int(w) for w in first.stdout.strip().splitlines()[-1].split("]")[0].strip("[").split(",")]
+    assert all(w in (64, 128, 256) for w in widths) and widths[2] == 64  # the 31-wide PSF: one tile per item
     second = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=600)
     assert second.returncode == 0, second.stderr
     assert second.stdout.strip() == first.stdout.strip()
     assert len(cache.read_text().strip().splitlines()) == 1  # read from the cache, nothing re-measured
+
+
+@pytest.mark.parametrize("grouping", [0, 1, 2, 3])
+def test_every_item_shape_matches_the_single_image_path(cuda, grouping):
+    # the autotuner's item shapes (1, 2 or 4 tiles per item by PSF width) pinned one by one,
+    # with both queue orders and 1 and 4 CTAs per SM: the same bits as the single-image path
+    obs, psfs = make_batch(seed=3)
+    singles = []
+    for o, p in zip(obs, psfs):
+        rl = iane_gb300.RichardsonLucy(to_gpu(p), o.shape)
+        e = empty_like_np(o.shape, np.float32)
+        rl.run(to_gpu(o), e, 4, 1e-6, init=rl.INIT_MEAN)
+        singles.append(to_host(e))
+        rl.close()
+    batch = iane_gb300.RichardsonLucyBatch([to_gpu(p) for p in psfs], [o.shape for o in obs])
+    for bps, order in ((1, 0), (4, 1)):
+        batch.configure(bps, order, grouping)
+        assert batch.launch_config() == (bps, order, grouping)
+        widths = batch.tile_widths()
+        assert all(w in (64, 128, 256) for w in widths)
+        got = run_batch(batch, obs, 4, iane_gb300.RichardsonLucy.INIT_MEAN)
+        for g, s in zip(got, singles):
+            assert np.array_equal(g, s)
+    with pytest.raises(iane_gb300.IaneError):
+        batch.configure(1, 0, 4)
+    batch.close()
