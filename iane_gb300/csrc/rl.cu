@@ -148,10 +148,21 @@ __global__ void rl_mean_kernel(DevView obs, double* partials, unsigned int* coun
 		last = atomicAdd(counter, 1u) == gridDim.x - 1;
 	}
 	__syncthreads();
-	if (last && threadIdx.x == 0) {
-		__threadfence();
+	if (!last) {
+		return;
+	}
+	// the last block combines the block partials: each thread a strided share, then the warps
+	// and the block (a fixed order, so the start value is deterministic)
+	__threadfence();
+	double t = 0.0;
+	for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) t += __ldcg(&partials[b]);
+	for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+	__syncthreads();
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+	__syncthreads();
+	if (threadIdx.x == 0) {
 		double total = 0.0;
-		for (unsigned int b = 0; b < gridDim.x; ++b) total += __ldcg(&partials[b]);
+		for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) total += red[w];
 		const float mean = static_cast<float>(total / static_cast<double>(n));
 		*start = mean > eps ? mean : eps;
 		*counter = 0u;
