@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(kFThreads) separable_fast_kernel(const __grid_
 //     within R of the image are listed (the others feed no stored output); for images of at
 //     least 16 x 16 their source cells lie inside the tile;
 //   * only the thread that issues a plane's TMA maps its z coordinate.
-constexpr int kRBuf = 3; // tile buffers: the iteration's two planes and the next one
+constexpr int kRBuf = 4; // tile buffers: the iteration's two planes and the next two
 
 template<int R>
 struct RingGeom {
@@ -416,8 +416,7 @@ __global__ void __launch_bounds__(kFThreads, R <= 3 ? 3 : 2) separable_ring_kern
 		tma_load_3d(A + b * G::A_FLOATS, &map, x0 - G::RA, y0 - R, present ? zi : z, &bars[b]);
 	};
 	if (tid == 0) {
-		issue(0);
-		issue(1);
+		for (int m = 0; m < kRBuf && m < 2 * npairs; ++m) issue(m);
 	}
 	bool ok = true;
 	auto wait_fix = [&](int m) {
@@ -456,10 +455,7 @@ __global__ void __launch_bounds__(kFThreads, R <= 3 ? 3 : 2) separable_ring_kern
 
 	for (int pp = 0; pp < npairs; ++pp) {
 		const int p = 2 * pp; // planes p and p + 1
-		// plane p + 2 goes to the buffer of plane p - 1, whose axis-0 reads ended before the
-		// first barrier of the previous iteration. Only planes this block waits for are
-		// issued: no copy may still be in flight when the block exits.
-		if (tid == 0 && p + 2 < 2 * npairs) issue(p + 2);
+		// planes p + 2 and p + 3 are in flight while p and p + 1 are filtered
 		wait_fix(p);
 		wait_fix(p + 1);
 		if (nfix > 0) __syncthreads(); // fixed tiles visible to all
@@ -491,8 +487,12 @@ __global__ void __launch_bounds__(kFThreads, R <= 3 ? 3 : 2) separable_ring_kern
 			*reinterpret_cast<float4*>(Bbuf + pl * G::B_FLOATS + r * kFX + 4 * xq) = make_float4(o[0], o[1], o[2], o[3]);
 		}
 		__syncthreads(); // B complete; the tiles of planes p, p + 1 are free
-		// plane p + 3 goes to the buffer of plane p, just released
-		if (tid == 0 && p + 3 < 2 * npairs) issue(p + 3);
+		// planes p + 4 and p + 5 go to their buffers, just released. Only planes this block waits
+		// for are issued: no copy may still be in flight when the block exits.
+		if (tid == 0) {
+			if (p + 4 < 2 * npairs) issue(p + 4);
+			if (p + 5 < 2 * npairs) issue(p + 5);
+		}
 #pragma unroll
 		for (int pl = 0; pl < 2; ++pl) {
 			const float* B = Bbuf + pl * G::B_FLOATS;
