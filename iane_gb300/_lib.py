@@ -55,7 +55,7 @@ def lib() -> ctypes.CDLL:
     l.iane_gb_last_error.restype = ctypes.c_size_t
     l.iane_gb_device_status.argtypes = [vp]
     l.iane_gb_device_status.restype = ctypes.c_int
-    l.iane_gb_wait_probe.argtypes = [ctypes.c_uint, vp]
+    l.iane_gb_wait_probe.argtypes = [ctypes.c_uint, ctypes.c_int, vp]
     l.iane_gb_wait_probe.restype = ctypes.c_int
     l.iane_gb_fp32_peak_probe.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
     l.iane_gb_fp32_peak_probe.restype = ctypes.c_int

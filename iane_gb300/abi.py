@@ -28,6 +28,9 @@ ERODE, DILATE, OPENING, CLOSING = 0, 1, 2, 3
 MORPHOLOGY_OPS = {"erode": ERODE, "dilate": DILATE, "opening": OPENING, "closing": CLOSING}
 RL_BF16_TENSOR = 1
 RL_PER_PASS = 2
+PROBE_MBARRIER = 0
+PROBE_COUNTER = 1
+PROBE_COUNTER_ABORT = 2
 BATCH_AUTOTUNE = 1
 
 OK = 0

@@ -262,6 +262,31 @@ __global__ void wait_probe_kernel(int* status, unsigned long long limit_ns)
 	}
 }
 
+// The persistent queues' dependency wait: thread 0 waits for a completion counter in global
+// memory (as the queues' counters are; the probe's own pair of device words, so probes must not
+// overlap) that nothing raises. Kind 1: the bound runs out, the wait records
+// IANE_GB_DEVICE_TIMEOUT and raises the abort flag. Kind 2: warp 1 raises the abort flag after
+// 1 ms of global time, and the wait must return then without recording anything.
+__device__ unsigned int g_probe_counter;
+__device__ int g_probe_abort;
+
+__global__ void counter_probe_kernel(int* status, unsigned long long limit_ns, int kind)
+{
+	if (threadIdx.x == 0) {
+		g_probe_counter = 0u;
+		g_probe_abort = 0;
+		__threadfence();
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		wait_counter(&g_probe_counter, 1u, &g_probe_abort, status, limit_ns);
+	} else if (kind == 2 && threadIdx.x == 32) {
+		const uint64_t t0 = global_ns();
+		while (global_ns() - t0 < 1000000ull) __nanosleep(1000);
+		atomicExch(&g_probe_abort, 1);
+	}
+}
+
 int convolve_checked(const DevView& s, const DevView& k, const DevView& d, int border, unsigned flags, void* stream,
 	const TexSource* tex)
 {
@@ -350,14 +375,22 @@ int convolve_checked(const DevView& s, const DevView& k, const DevView& d, int b
 
 extern "C" {
 
-int iane_gb_wait_probe(unsigned int limit_us, void* stream)
+int iane_gb_wait_probe(unsigned int limit_us, int kind, void* stream)
 {
 	if (limit_us == 0 || limit_us > 10000000u) {
 		return fail(IANE_GB_INVALID_ARGUMENT, "wait probe: the limit is 1 us .. 10 s");
 	}
+	if (kind < IANE_GB_PROBE_MBARRIER || kind > IANE_GB_PROBE_COUNTER_ABORT) {
+		return fail(IANE_GB_INVALID_ARGUMENT, "wait probe: unknown kind");
+	}
 	int* status = device_status_ptr();
 	if (!status) return IANE_GB_CUDA_ERROR;
-	wait_probe_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(status, 1000ull * limit_us);
+	const cudaStream_t st = static_cast<cudaStream_t>(stream);
+	if (kind == IANE_GB_PROBE_MBARRIER) {
+		wait_probe_kernel<<<1, 32, 0, st>>>(status, 1000ull * limit_us);
+	} else {
+		counter_probe_kernel<<<1, 64, 0, st>>>(status, 1000ull * limit_us, kind);
+	}
 	IANE_GB_CUDA(cudaGetLastError(), "wait probe: launch");
 	return IANE_GB_OK;
 }

@@ -332,9 +332,10 @@ __device__ __forceinline__ void fence_proxy_async_global()
 	asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
-// Bounded wait until *word >= need. False if the run was aborted or the wait gave up (which it
-// records in the status word and turns into an abort).
-__device__ __forceinline__ bool wait_counter(const unsigned int* word, unsigned int need, int* abort, int* status)
+// Bounded wait until *word >= need. False if the run was aborted or the wait gave up after
+// `limit_ns` of global time (which it records in the status word and turns into an abort).
+__device__ __forceinline__ bool wait_counter(const unsigned int* word, unsigned int need, int* abort, int* status,
+	uint64_t limit_ns = 2000000000ull)
 {
 	if (load_acquire(word) >= need) {
 		return true;
@@ -347,7 +348,7 @@ __device__ __forceinline__ bool wait_counter(const unsigned int* word, unsigned 
 		if (load_volatile(abort)) {
 			return false;
 		}
-		if ((i & 63u) == 0 && global_ns() - t0 > 2000000000ull) {
+		if ((i & 63u) == 0 && global_ns() - t0 > limit_ns) {
 			break;
 		}
 		__nanosleep(64);

@@ -102,11 +102,20 @@ size_t iane_gb_last_error(char* buf, size_t size);
  * IANE_GB_DEVICE_TIMEOUT if a bounded device-side wait of an earlier launch gave up. */
 int iane_gb_device_status(void* stream);
 
-/* Diagnostic: launch a kernel whose one wait never completes (an mbarrier nobody arrives on),
- * bounded to `limit_us` microseconds (1 .. 10^7). The kernel records IANE_GB_DEVICE_TIMEOUT in
- * the status word and ends; the next iane_gb_device_status reports it, and the context stays
- * usable. Every device-side wait of this library has the same bound (two seconds). */
-int iane_gb_wait_probe(unsigned int limit_us, void* stream);
+/* Diagnostic: launch a kernel with one device-side wait of the given kind, bounded to
+ * `limit_us` microseconds (1 .. 10^7):
+ *   IANE_GB_PROBE_MBARRIER: an mbarrier nobody arrives on;
+ *   IANE_GB_PROBE_COUNTER: a completion counter nothing raises (the persistent queues' wait);
+ *     the wait also raises the run's abort flag;
+ *   IANE_GB_PROBE_COUNTER_ABORT: the same counter, with another warp raising the abort flag
+ *     after 1 ms -- the wait returns then and records nothing.
+ * A wait that gives up records IANE_GB_DEVICE_TIMEOUT in the status word and the kernel ends;
+ * the next iane_gb_device_status reports it, and the context stays usable. Every device-side
+ * wait of this library has the same kind of bound (two seconds). */
+#define IANE_GB_PROBE_MBARRIER 0
+#define IANE_GB_PROBE_COUNTER 1
+#define IANE_GB_PROBE_COUNTER_ABORT 2
+int iane_gb_wait_probe(unsigned int limit_us, int kind, void* stream);
 
 /* Diagnostic: measured FP32 fused multiply-add throughput of the current device in TFLOP/s
  * (2 flops per FMA), the ceiling of FP32-pipe-bound convolutions. paired = 0 issues scalar

@@ -89,10 +89,12 @@ def test_rl_prepare_rejects_even_psf_without_gpu():
     assert not handle.value
 
 
-def test_wait_probe_checks_its_limit_before_any_launch():
+def test_wait_probe_checks_its_limit_and_kind_before_any_launch():
     lib = iane_gb300.lib()
     for bad in (0, 10000001):
-        assert lib.iane_gb_wait_probe(bad, None) == iane_gb300.abi.INVALID_ARGUMENT
+        assert lib.iane_gb_wait_probe(bad, 0, None) == iane_gb300.abi.INVALID_ARGUMENT
+    for kind in (-1, 3):
+        assert lib.iane_gb_wait_probe(1000, kind, None) == iane_gb300.abi.INVALID_ARGUMENT
 
 
 def test_rgb8_and_texture_argument_checks():
