@@ -26,8 +26,8 @@
 // covers the same 32 x 32 per warp and reads the same tile (its width does not depend on RX):
 // per kernel row it loads the taps once for 16 x 2 = 32 FMAs per tap instead of twice, and
 // the interior input rows, which feed both output rows, run without the kernel-row checks.
-// The persistent RL kernel uses it; the sums are the same bits in either geometry (each
-// output's taps are added in the same order).
+// The persistent RL kernel and the 3-D fast convolve up to 15 wide use it; the sums are the
+// same bits in either geometry (each output's taps are added in the same order).
 // Per kernel plane each output accumulates its ky*kx taps into a plane partial that is
 // added to the total afterwards (two-level FP32 summation), which keeps the rounding error
 // of a 1575-tap sum near 1e-6 relative. Single-plane kernels (SINGLE) sum straight into the
