@@ -713,8 +713,11 @@ static int rl_prepare_impl(const iane_gb_view* psf, int rank, const int32_t* ext
 	const int t = plan->small_tiles ? 32 : 64;
 	plan->pass_blocks = static_cast<long long>((ext[0] + t - 1) / t) * ((ext[1] + t - 1) / t) * ext[2];
 	const long long mean_blocks = 8LL * device_sm_count();
+	// partials: the mean's blocks, or 3 doubles per pass B block -- two such buffers (one per
+	// iteration parity) for the persistent run's statistics
+	const long long stat_parts = plan->pass_blocks * 3 * (plan->small_tiles ? 1 : 2);
 	plan->parts_bytes = round_up(static_cast<size_t>(
-		(plan->pass_blocks * 3 > mean_blocks ? plan->pass_blocks * 3 : mean_blocks) * sizeof(double)), kAlign);
+		(stat_parts > mean_blocks ? stat_parts : mean_blocks) * sizeof(double)), kAlign);
 	plan->sync_bytes = round_up(rl_persist_sync_bytes(ext[2]), kAlign);
 	plan->scratch_bytes = 2 * plan->image_bytes + plan->parts_bytes + 2 * kAlign + plan->sync_bytes;
 	if (bf16) {
@@ -898,11 +901,10 @@ int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const ia
 	eb.out = est.ptr;
 	eb.out_u8 = est.dtype == IANE_GB_U8;
 
-	// One persistent launch for the whole run (rl_persist.cuh) unless the caller wants per-iteration
-	// statistics (their deterministic block-order reduction closes each pass B launch), the image is
-	// small enough for 32 x 32 tiles, or the plan asks for one launch per pass.
+	// One persistent launch for the whole run (rl_persist.cuh) unless the image is small enough for
+	// 32 x 32 tiles or the plan asks for one launch per pass.
 	const long long tiles_x = (nx + 63) / 64, tiles_y = (ny + 63) / 64;
-	const bool persistent = !plan->per_pass && !plan->small_tiles && stats == nullptr && iterations > 0 &&
+	const bool persistent = !plan->per_pass && !plan->small_tiles && iterations > 0 &&
 		tiles_x * tiles_y * nz * 2LL * iterations < (1LL << 31);
 	if (persistent) {
 		unsigned int* sync = reinterpret_cast<unsigned int*>(base + 2 * plan->image_bytes + plan->parts_bytes + kAlign);
@@ -923,6 +925,10 @@ int iane_gb_rl_run(iane_gb_rl_plan* plan, const iane_gb_view* observed, const ia
 		pa.queue = sync;
 		pa.abort = reinterpret_cast<int*>(sync + 1);
 		pa.done = sync + 2;
+		pa.parts = parts;
+		pa.stats = stats;
+		pa.stat_count = sync + 2 + nz;
+		pa.stat_done = sync + 4 + nz;
 		IANE_GB_CUDA(cudaMemsetAsync(sync, 0, rl_persist_sync_bytes(nz), st), "rl_run: clear queue");
 		return launch_rl_persist(kx, pa, st);
 	}

@@ -220,9 +220,10 @@ int iane_gb_rl_prepare(const iane_gb_view* psf, int rank, const int32_t* extent,
  * 17 wide. No counterpart in the reference, which convolves in FP64. */
 #define IANE_GB_RL_BF16_TENSOR 1u
 
-/* FP32 path: one launch per pass (two per iteration) instead of one persistent launch for
- * the whole run. The results are the same bits; runs that return statistics, and images
- * small enough for 32 x 32 tiles, always take one launch per pass. */
+/* FP32 path: one launch per pass (two per iteration) instead of one persistent launch for the
+ * whole run. The estimates are the same bits (the statistics agree to rounding: the two
+ * schedules group the FP32 partial sums differently); images small enough for 32 x 32 tiles
+ * always take one launch per pass. */
 #define IANE_GB_RL_PER_PASS 2u
 
 /* iane_gb_rl_prepare with flags (0, or IANE_GB_RL_BF16_TENSOR and/or IANE_GB_RL_PER_PASS). */

@@ -88,3 +88,29 @@ def test_persistent_matches_oracle(cuda):
     est = run(obs, psf, 4, 1, per_pass=False)
     assert rel_l2(est, ref) <= TOL
     assert float(np.max(np.abs(est.astype(np.float64) - ref))) <= TOL * float(np.max(np.abs(ref)))
+
+
+def test_persistent_statistics_match_per_pass_and_oracle(cuda):
+    # per-iteration flux and relative change from the persistent run: the same estimate bits as
+    # one launch per pass, statistics equal to rounding (the schedules group the FP32 partial
+    # sums differently) and to the oracle's within the RL test's bars
+    t = torch()
+    shape, psf = (18, 200, 280), gaussian((5, 7, 7), (1.0, 1.5, 1.5))  # 4 x 5 x 18 = 360 tiles
+    obs = observed(shape, psf, 9)
+    iters = 5
+    results = []
+    for per_pass in (False, True):
+        rl = iane_gb300.RichardsonLucy(to_gpu(psf), shape, per_pass=per_pass)
+        est = empty_like_np(shape, np.float32)
+        st = t.zeros(2 * iters, dtype=t.float64, device="cuda")
+        rl.run(to_gpu(obs), est, iters, 1e-6, init=rl.INIT_MEAN, stats=st)
+        iane_gb300.device_status()
+        results.append((to_host(est), to_host(st).reshape(-1, 2)))
+        rl.close()
+    (e_p, s_p), (e_s, s_s) = results
+    assert np.array_equal(e_p, e_s)
+    assert np.allclose(s_p, s_s, rtol=1e-6, atol=0.0)
+    ref, ref_stats = oracle.rl(obs, psf, iters, 1e-6, init=1, with_stats=True)
+    assert rel_l2(e_p, ref) <= TOL
+    assert np.allclose(s_p[:, 0], ref_stats[:, 0], rtol=1e-5)
+    assert np.allclose(s_p[:, 1], ref_stats[:, 1], rtol=1e-3, atol=1e-7)
