@@ -13,7 +13,10 @@ The simulation takes items in queue order into free CTAs, starts an item when it
 holds, and checks at every start and finish that the rule really orders the data: every plane
 an item reads holds the previous phase's result (read after write), no item overwrites a plane
 that an item of the previous phase is still reading (write after read), a counter that reached
-p * tiles means phases < p are complete on that plane, and the run never stalls (progress)."""
+p * tiles means phases < p are complete on that plane, and the run never stalls (progress).
+With per-iteration statistics the volume's pass B items also write partials into a buffer per
+iteration parity, combined when an iteration's last pass B item finishes: no partial is
+overwritten before its iteration is combined, and iterations are combined in order."""
 from __future__ import annotations
 
 import heapq
@@ -71,17 +74,26 @@ def simulate(items, ready, reads, writes, finish, ctas, seed):
     return done
 
 
-def volume_case(nz, kz, tiles, phases, ctas, seed):
+def volume_case(nz, kz, tiles, phases, ctas, seed, stats=False, stats_wait=True):
     rz = kz // 2
     items = [(p, z, t) for p in range(phases) for z in range(nz) for t in range(tiles)]
     done_count = [0] * nz
     completed = set()
+    # statistics: pass B items write partials[parity][item]; the last pass B item of iteration t
+    # combines partials[t % 2] when it finishes; pass B of iteration t >= 2 waits for iteration
+    # t - 2 to be combined
+    per_phase = nz * tiles
+    partial_of = {}       # (parity, item index) -> iteration whose partial is stored
+    stat_count = [0, 0]
+    combined = [0]        # iterations combined so far
 
     def window(z):
         return range(max(0, z - rz), min(nz, z + rz + 1))
 
     def ready(it):
         p, z, _ = it
+        if stats and stats_wait and p % 2 == 1 and p // 2 >= 2 and combined[0] < p // 2 - 1:
+            return False
         return p == 0 or all(done_count[w] >= p * tiles for w in window(z))
 
     def reads(it):
@@ -99,7 +111,22 @@ def volume_case(nz, kz, tiles, phases, ctas, seed):
         return {("ratio" if p % 2 == 0 else "est", (z, t))}
 
     def finish(it):
-        p, z, _ = it
+        p, z, t = it
+        if stats and p % 2 == 1:
+            n = p // 2
+            # the slot may only be overwritten once iteration n - 2 has been combined
+            prev = partial_of.get((n % 2, z * tiles + t))
+            assert prev is None or prev == n - 2
+            assert prev is None or combined[0] >= n - 1
+            partial_of[(n % 2, z * tiles + t)] = n
+            stat_count[n % 2] += 1
+            if stat_count[n % 2] == per_phase:
+                # combine: every partial of the parity is this iteration's, and iterations
+                # are combined in order
+                assert all(partial_of[(n % 2, k)] == n for k in range(per_phase))
+                assert combined[0] == n
+                stat_count[n % 2] = 0
+                combined[0] = n + 1
         done_count[z] += 1
         completed.add(it)
         # a counter that reached q * tiles means phases < q are complete on that plane
@@ -108,6 +135,8 @@ def volume_case(nz, kz, tiles, phases, ctas, seed):
 
     out = simulate(items, ready, reads, writes, finish, ctas, seed)
     assert len(out) == len(items)
+    if stats:
+        assert combined[0] == phases // 2
 
 
 def batch_case(tiles_per_image, phases, ctas, seed):
@@ -144,6 +173,21 @@ def batch_case(tiles_per_image, phases, ctas, seed):
 def test_volume_schedule_orders_every_access(nz, kz, tiles, ctas):
     for seed in range(3):
         volume_case(nz, kz, tiles, phases=6, ctas=ctas, seed=seed)
+
+
+@pytest.mark.parametrize("ctas", [1, 2, 7, 40, 200])
+@pytest.mark.parametrize("nz,kz,tiles", [(6, 3, 2), (9, 7, 1), (2, 5, 3), (20, 1, 1), (24, 3, 1)])
+def test_volume_statistics_combine_every_iteration_in_order(nz, kz, tiles, ctas):
+    for seed in range(3):
+        volume_case(nz, kz, tiles, phases=10, ctas=ctas, seed=seed, stats=True)
+
+
+def test_statistics_without_their_wait_fail():
+    # the checks have teeth: with planes that do not depend on each other (kz = 1), pass B of
+    # iteration t + 2 can overwrite a partial before iteration t is combined unless it waits
+    with pytest.raises(AssertionError):
+        for seed in range(20):
+            volume_case(20, 1, 1, phases=10, ctas=200, seed=seed, stats=True, stats_wait=False)
 
 
 @pytest.mark.parametrize("ctas", [1, 3, 8, 64])
