@@ -131,7 +131,7 @@ std::vector<BatchItem> make_items(const std::vector<int>& nx, const std::vector<
 	for (int i : idx) {
 		const int tx = tiles_of(nx[i]), ty = tiles_of(ny[i]), s = tiles_per_item(kx[i], group);
 		for (int r = 0; r < ty; ++r) {
-			for (int c = 0; c < tx; c += s) items.push_back(BatchItem{i, r * tx + c, std::min(s, tx - c)});
+			for (int c = 0; c < tx; c += s) items.push_back(BatchItem{i, r * tx + c, std::min(s, tx - c), tx * ty});
 		}
 	}
 	return items;

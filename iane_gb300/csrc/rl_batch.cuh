@@ -49,6 +49,7 @@ struct BatchItem {
 	int image;
 	int tile;
 	int count;
+	int image_tiles; // the image's 64x64 tiles (its completions per phase), read at hand-off
 };
 
 // Device words of a run, cleared before the launch: the queue counter, the abort flag and one

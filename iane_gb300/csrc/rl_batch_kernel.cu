@@ -51,10 +51,13 @@ __global__ void __launch_bounds__(128) batch_persistent_kernel(const BatchImage*
 			if (go) {
 				const int phase = static_cast<int>(k / static_cast<unsigned int>(items_per_phase));
 				const BatchItem w = items[k - static_cast<unsigned int>(phase) * items_per_phase];
+				// the item's tensor map into the descriptor cache while the wait and the taps proceed
+				const CUtensorMap* map = (phase & 1) ? &images[w.image].map_ratio : &images[w.image].map_est;
+				asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 				if (phase > 0) {
 					// the image's previous phase complete (bounded: a wait that gives up aborts the run)
-					go = wait_counter(&sync.done[w.image], static_cast<unsigned int>(phase) * images[w.image].tiles,
-						sync.abort, status);
+					go = wait_counter(&sync.done[w.image], static_cast<unsigned int>(phase) * w.image_tiles, sync.abort,
+						status);
 					fence_proxy_async_global(); // the image's previous phase, written by generic stores, before TMA
 				}
 			}
