@@ -17,6 +17,11 @@ int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevVi
 	if (ky > 63 || src.ext[1] > 65535 * 32 || src.ext[2] > 65535) {
 		return IANE_GB_UNSUPPORTED;
 	}
+	// large 2-D f32 images with small square kernels: the row-strip kernel (same sums)
+	if (!tex) {
+		const int rows = launch_direct_rows(src, kernel, dst, border, stream);
+		if (rows != IANE_GB_UNSUPPORTED) return rows;
+	}
 	// Small single-plane jobs (too few 64x64 tiles for every SM, and under 5e7 tap-products):
 	// the one-warp blocks of 32x32 tiles are latency-bound there, and the generic kernel (one
 	// output per thread, 256-thread blocks, FP32 sums) with many times the warps per SM is

@@ -209,13 +209,11 @@ int launch_rows(const CUtensorMap& map, const RowsArgs& args, cudaStream_t strea
 	IANE_GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRowsThreads, smem),
 		"separable rows: occupancy");
 	const int strips = (args.nx + kRowsSW - 1) / kRowsSW;
-	// chunks so that the grid is two full waves when the image is tall enough, else chunks of at
-	// least four steps
+	// chunks of at least four steps that fill whole waves of resident blocks
 	const long long slots = static_cast<long long>(std::max(per_sm, 1)) * device_sm_count();
-	long long chunks = (2 * slots + strips - 1) / strips;
-	chunks = std::min<long long>(chunks, std::max(1, args.ny / (4 * kRowsStep)));
+	const int chunks = strip_chunks(strips, args.ny, slots, kRowsStep);
 	RowsArgs a = args;
-	a.chunk = static_cast<int>((args.ny + chunks - 1) / chunks);
+	a.chunk = (args.ny + chunks - 1) / chunks;
 	const dim3 grid(strips, static_cast<unsigned int>((args.ny + a.chunk - 1) / a.chunk));
 	kernel<<<grid, kRowsThreads, smem, stream>>>(map, a);
 	IANE_GB_CUDA(cudaGetLastError(), "separable rows: launch");
