@@ -376,12 +376,18 @@ def measure_hbm_legs(dev, stream, reps=20, cpu=True):
     # bandwidth at a large 2-D size (256 MiB in, 256 MiB out: larger than L2)
     big = torch.rand((8192, 8192), generator=gen, device=dev, dtype=torch.float32)
     dbig = torch.empty_like(big)
-    for name, fn in (("direct_8192^2_7x7_mirror", lambda: iane_gb300.convolve(big, g2, dbig, "mirror", stream=stream)),
-                     ("separable_8192^2_7x7_mirror",
-                      lambda: iane_gb300.convolve_separable(big, [g1, g1], dbig, "mirror", stream=stream))):
+    fp32 = fp32_peak_tflops(dev)["peak"]
+    for name, fn, flop in (("direct_8192^2_7x7_mirror", lambda: iane_gb300.convolve(big, g2, dbig, "mirror", stream=stream),
+                            2 * 49),
+                           ("separable_8192^2_7x7_mirror",
+                            lambda: iane_gb300.convolve_separable(big, [g1, g1], dbig, "mirror", stream=stream), 2 * 14)):
         ms = timed(fn)
         gbs = 8.0 * big.numel() / (ms / 1e3) / 1e9
-        out[name] = {"ms": ms, "gvoxel_s": big.numel() / (ms / 1e3) / 1e9, "gbs": gbs, "hbm_frac": gbs / hbm}
+        tflops = flop * big.numel() / (ms / 1e3) / 1e12
+        # 98 flop per 8 bytes puts the direct 7x7 filter at this GPU's FP32 / HBM ridge: both
+        # fractions are stated
+        out[name] = {"ms": ms, "gvoxel_s": big.numel() / (ms / 1e3) / 1e9, "gbs": gbs, "hbm_frac": gbs / hbm,
+                     "tflops": tflops, "fp32_frac": tflops / fp32}
     del big, dbig
     return out
 
