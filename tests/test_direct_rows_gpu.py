@@ -96,3 +96,24 @@ def test_neighbouring_cases_take_the_other_kernels(cuda, shape, kshape):
     out = empty_like_np(src.shape, np.float32)
     iane_gb300.convolve(to_gpu(src), to_gpu(taps), out, "mirror")
     assert rel_err_bound(to_host(out), ref, magnitude(src, taps, "mirror")) <= 1e-5
+
+
+def test_non_finite_pixels_match_the_tiled_kernel_bit_for_bit(cuda):
+    # NaN and +-Inf samples (near the image's corners, edges and interior) propagate through
+    # the same FMAs in the same order in both kernels: the outputs' bit patterns are equal
+    rng = np.random.default_rng(90)
+    shape = (2085, 2100)
+    src = rng.random(shape, dtype=np.float32)
+    for (y, x), v in {(0, 0): np.nan, (1, 2098): np.inf, (2084, 5): -np.inf, (1000, 1000): np.nan,
+                      (1500, 64): np.inf, (31, 127): -np.inf, (2083, 2099): np.nan}.items():
+        src[y, x] = v
+    taps = random_taps(7, 9)
+    g = to_gpu(taps)
+    for border in ("mirror", "zero"):
+        rows = empty_like_np(shape, np.float32)
+        iane_gb300.convolve(to_gpu(src), g, rows, border)
+        tiled = empty_like_np(shape, np.float32)
+        iane_gb300.convolve(misaligned_copy(src), g, tiled, border)
+        a, b = to_host(rows), to_host(tiled)
+        assert np.isnan(a).any() and np.isinf(a).any()
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
