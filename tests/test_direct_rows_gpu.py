@@ -20,7 +20,10 @@ from gpu_helpers import empty_like_np, gaussian, magnitude, to_gpu, to_host, tor
 pytestmark = pytest.mark.gpu
 
 CASES = [((2048, 2080), 7, "mirror"), ((2111, 2049), 5, "clamp"), ((2100, 2200), 3, "zero"),
-         ((1030, 4096), 7, "clamp"), ((2049, 2177), 7, "zero"), ((4100, 1025), 3, "mirror")]
+         ((1030, 4096), 7, "clamp"), ((2049, 2177), 7, "zero"), ((4100, 1025), 3, "mirror"),
+         # one strip that is both the first and the last; a last strip one column wide; the
+         # least height taken (four steps) in one chunk per strip
+         ((32769, 128), 7, "mirror"), ((16400, 257), 5, "clamp"), ((128, 32800), 3, "mirror")]
 
 
 def random_taps(k, seed):
