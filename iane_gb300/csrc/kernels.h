@@ -53,8 +53,9 @@ int convolve_checked(const DevView& s, const DevView& k, const DevView& d, int b
 int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevView& dst, int border,
 	cudaStream_t stream, const TexSource* tex = nullptr);
 
-// Row-strip direct FP32 convolution of large 2-D f32 images with square kernels of 3 to 7 taps
-// (direct_rows.cu); the same bits as the tiled kernel. IANE_GB_UNSUPPORTED without an error
+// Row-strip direct FP32 convolution of large 2-D f32 images (or stacks of 2-D planes under a
+// kernel one plane deep) with square kernels of 3 to 7 taps (direct_rows.cu); the same bits as
+// the tiled kernel. IANE_GB_UNSUPPORTED without an error
 // when the views or the kernel do not qualify.
 int launch_direct_rows(const DevView& src, const DevView& kernel, const DevView& dst, int border,
 	cudaStream_t stream);

@@ -1,5 +1,6 @@
 """The row-strip direct kernel (direct_rows.cu), which iane_gb_convolve takes for 2-D f32 images
-of at least 4 M pixels with square f32 kernels of 3, 5 or 7 taps.
+(or stacks of 2-D planes under a kernel one plane deep) of at least 4 M pixels with square f32
+kernels of 3, 5 or 7 taps.
 
 Against the oracle within the FP32 bar |gpu - ref| <= 1e-5 * conv(|src|, |k|) for the three
 borders, every kernel size, ragged image sizes and non-symmetric taps; bit for bit against the
@@ -23,19 +24,22 @@ CASES = [((2048, 2080), 7, "mirror"), ((2111, 2049), 5, "clamp"), ((2100, 2200),
          ((1030, 4096), 7, "clamp"), ((2049, 2177), 7, "zero"), ((4100, 1025), 3, "mirror"),
          # one strip that is both the first and the last; a last strip one column wide; the
          # least height taken (four steps) in one chunk per strip
-         ((32769, 128), 7, "mirror"), ((16400, 257), 5, "clamp"), ((128, 32800), 3, "mirror")]
+         ((32769, 128), 7, "mirror"), ((16400, 257), 5, "clamp"), ((128, 32800), 3, "mirror"),
+         # stacks of planes, each filtered on its own
+         ((3, 1400, 1500), 7, "mirror"), ((5, 1000, 900), 5, "clamp"), ((2, 2048, 2048), 3, "zero")]
 
 
-def random_taps(k, seed):
+def random_taps(k, seed, planes=False):
     rng = np.random.default_rng(seed)
-    return (rng.random((k, k), dtype=np.float32) - 0.3).astype(np.float32)
+    taps = (rng.random((k, k), dtype=np.float32) - 0.3).astype(np.float32)
+    return taps[None] if planes else taps
 
 
 @pytest.mark.parametrize("shape,k,border", CASES, ids=[f"{s}-{k}-{b}" for s, k, b in CASES])
 def test_against_oracle(cuda, shape, k, border):
     rng = np.random.default_rng(sum(shape) + k)
     src = rng.random(shape, dtype=np.float32) * 4.0 - 1.0
-    taps = random_taps(k, k + 11)
+    taps = random_taps(k, k + 11, planes=len(shape) == 3)
     ref = np.zeros(shape, np.float32)
     oracle.convolve(src, taps, ref, border)
     out = empty_like_np(shape, np.float32)
@@ -47,9 +51,9 @@ def test_against_oracle(cuda, shape, k, border):
 def misaligned_copy(src):
     """The same image in a buffer whose rows start 4 bytes past a 16-byte boundary."""
     t = torch()
-    ny, nx = src.shape
-    flat = t.zeros(ny * nx + 4, dtype=t.float32, device="cuda")
-    view = flat[1:1 + ny * nx].view(ny, nx)
+    n = src.size
+    flat = t.zeros(n + 4, dtype=t.float32, device="cuda")
+    view = flat[1:1 + n].view(*src.shape)
     view.copy_(to_gpu(src))
     assert view.data_ptr() % 16 == 4
     return view
@@ -88,9 +92,10 @@ def test_pitched_source_and_cropped_destination(cuda):
 
 
 @pytest.mark.parametrize("shape,kshape", [((2047, 2048), (7, 7)), ((2048, 2048), (7, 5)), ((2048, 2048), (9, 9)),
-                                          ((2, 2048, 2048), (1, 7, 7))])
+                                          ((2, 2048, 2048), (3, 7, 7)), ((2, 1024, 2047), (1, 7, 7))])
 def test_neighbouring_cases_take_the_other_kernels(cuda, shape, kshape):
-    # just under 4 M pixels, non-square, 9 x 9 and a stack of planes: the tiled kernel, same bar
+    # just under 4 M pixels (one plane or a stack), non-square, 9 x 9 and a kernel three planes
+    # deep: the tiled kernel, same bar
     rng = np.random.default_rng(sum(shape))
     src = rng.random(shape, dtype=np.float32)
     taps = (rng.random(kshape, dtype=np.float32) - 0.3).astype(np.float32)
@@ -120,3 +125,16 @@ def test_non_finite_pixels_match_the_tiled_kernel_bit_for_bit(cuda):
         a, b = to_host(rows), to_host(tiled)
         assert np.isnan(a).any() and np.isinf(a).any()
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_stack_equals_the_tiled_kernel_bit_for_bit(cuda):
+    rng = np.random.default_rng(91)
+    src = rng.random((3, 1200, 1300), dtype=np.float32)
+    taps = gaussian((1, 7, 7), (1.0, 1.7, 2.1))
+    g = to_gpu(taps)
+    for border in ("mirror", "clamp"):
+        rows = empty_like_np(src.shape, np.float32)
+        iane_gb300.convolve(to_gpu(src), g, rows, border)
+        tiled = empty_like_np(src.shape, np.float32)
+        iane_gb300.convolve(misaligned_copy(src), g, tiled, border)
+        assert np.array_equal(to_host(rows), to_host(tiled))
