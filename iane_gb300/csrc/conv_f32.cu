@@ -17,7 +17,7 @@ int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevVi
 	if (ky > 63 || src.ext[1] > 65535 * 32 || src.ext[2] > 65535) {
 		return IANE_GB_UNSUPPORTED;
 	}
-	// large 2-D f32 images with small square kernels: the row-strip kernel (same sums)
+	// large 2-D f32 images with kernels up to 7 x 7: the row-strip kernel (same sums)
 	if (!tex) {
 		const int rows = launch_direct_rows(src, kernel, dst, border, stream);
 		if (rows != IANE_GB_UNSUPPORTED) return rows;

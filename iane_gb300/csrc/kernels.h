@@ -54,8 +54,8 @@ int launch_conv_f32_tiled(const DevView& src, const DevView& kernel, const DevVi
 	cudaStream_t stream, const TexSource* tex = nullptr);
 
 // Row-strip direct FP32 convolution of large 2-D f32 images (or stacks of 2-D planes under a
-// kernel one plane deep) with square kernels of 3 to 7 taps (direct_rows.cu); the same bits as
-// the tiled kernel. IANE_GB_UNSUPPORTED without an error
+// kernel one plane deep) with kernels of odd extents up to 7, line filters included
+// (direct_rows.cu); the same bits as the tiled kernel. IANE_GB_UNSUPPORTED without an error
 // when the views or the kernel do not qualify.
 int launch_direct_rows(const DevView& src, const DevView& kernel, const DevView& dst, int border,
 	cudaStream_t stream);

@@ -1,6 +1,6 @@
 """The row-strip direct kernel (direct_rows.cu), which iane_gb_convolve takes for 2-D f32 images
-(or stacks of 2-D planes under a kernel one plane deep) of at least 4 M pixels with square f32
-kernels of 3, 5 or 7 taps.
+(or stacks of 2-D planes under a kernel one plane deep) of at least 4 M pixels with f32 kernels
+of odd extents up to 7 (square, non-square and line filters).
 
 Against the oracle within the FP32 bar |gpu - ref| <= 1e-5 * conv(|src|, |k|) for the three
 borders, every kernel size, ragged image sizes and non-symmetric taps; bit for bit against the
@@ -20,26 +20,32 @@ from gpu_helpers import empty_like_np, gaussian, magnitude, to_gpu, to_host, tor
 
 pytestmark = pytest.mark.gpu
 
+# kernel extents k: an int for square kernels, else (ky, kx)
 CASES = [((2048, 2080), 7, "mirror"), ((2111, 2049), 5, "clamp"), ((2100, 2200), 3, "zero"),
          ((1030, 4096), 7, "clamp"), ((2049, 2177), 7, "zero"), ((4100, 1025), 3, "mirror"),
          # one strip that is both the first and the last; a last strip one column wide; the
          # least height taken (four steps) in one chunk per strip
          ((32769, 128), 7, "mirror"), ((16400, 257), 5, "clamp"), ((128, 32800), 3, "mirror"),
          # stacks of planes, each filtered on its own
-         ((3, 1400, 1500), 7, "mirror"), ((5, 1000, 900), 5, "clamp"), ((2, 2048, 2048), 3, "zero")]
+         ((3, 1400, 1500), 7, "mirror"), ((5, 1000, 900), 5, "clamp"), ((2, 2048, 2048), 3, "zero"),
+         # non-square kernels and line filters
+         ((2050, 2100), (1, 7), "mirror"), ((2100, 2050), (7, 1), "clamp"), ((2049, 2111), (3, 7), "zero"),
+         ((2111, 2049), (5, 3), "mirror"), ((2048, 2080), (7, 5), "clamp"), ((3, 1400, 1500), (1, 5), "mirror")]
 
 
 def random_taps(k, seed, planes=False):
     rng = np.random.default_rng(seed)
-    taps = (rng.random((k, k), dtype=np.float32) - 0.3).astype(np.float32)
+    shape = (k, k) if isinstance(k, int) else k
+    taps = (rng.random(shape, dtype=np.float32) - 0.3).astype(np.float32)
     return taps[None] if planes else taps
 
 
-@pytest.mark.parametrize("shape,k,border", CASES, ids=[f"{s}-{k}-{b}" for s, k, b in CASES])
+@pytest.mark.parametrize("shape,k,border", CASES, ids=[f"{s}-{k}-{b}".replace(" ", "") for s, k, b in CASES])
 def test_against_oracle(cuda, shape, k, border):
-    rng = np.random.default_rng(sum(shape) + k)
+    kseed = k if isinstance(k, int) else 10 * k[0] + k[1]
+    rng = np.random.default_rng(sum(shape) + kseed)
     src = rng.random(shape, dtype=np.float32) * 4.0 - 1.0
-    taps = random_taps(k, k + 11, planes=len(shape) == 3)
+    taps = random_taps(k, kseed + 11, planes=len(shape) == 3)
     ref = np.zeros(shape, np.float32)
     oracle.convolve(src, taps, ref, border)
     out = empty_like_np(shape, np.float32)
@@ -59,12 +65,13 @@ def misaligned_copy(src):
     return view
 
 
-@pytest.mark.parametrize("k,border", [(7, "mirror"), (7, "clamp"), (5, "zero"), (3, "mirror")])
+@pytest.mark.parametrize("k,border", [(7, "mirror"), (7, "clamp"), (5, "zero"), (3, "mirror"), ((1, 7), "mirror"),
+                                      ((7, 3), "clamp"), ((5, 1), "mirror")])
 def test_whole_image_equals_the_tiled_kernel_bit_for_bit(cuda, k, border):
-    rng = np.random.default_rng(40 + k)
+    rng = np.random.default_rng(40 + (k if isinstance(k, int) else 10 * k[0] + k[1]))
     shape = (2085, 2100)
     src = rng.random(shape, dtype=np.float32)
-    taps = gaussian((k, k), (k / 4.0, k / 3.0)) if k > 3 else random_taps(k, 3)
+    taps = gaussian((k, k), (k / 4.0, k / 3.0)) if k in (5, 7) else random_taps(k, 3)
     g = to_gpu(taps)
     rows = empty_like_np(shape, np.float32)
     iane_gb300.convolve(to_gpu(src), g, rows, border)           # row-strip kernel
@@ -91,10 +98,10 @@ def test_pitched_source_and_cropped_destination(cuda):
     assert float(outside.abs().max()) == 0.0
 
 
-@pytest.mark.parametrize("shape,kshape", [((2047, 2048), (7, 7)), ((2048, 2048), (7, 5)), ((2048, 2048), (9, 9)),
+@pytest.mark.parametrize("shape,kshape", [((2047, 2048), (7, 7)), ((2048, 2048), (9, 5)), ((2048, 2048), (9, 9)),
                                           ((2, 2048, 2048), (3, 7, 7)), ((2, 1024, 2047), (1, 7, 7))])
 def test_neighbouring_cases_take_the_other_kernels(cuda, shape, kshape):
-    # just under 4 M pixels (one plane or a stack), non-square, 9 x 9 and a kernel three planes
+    # just under 4 M pixels (one plane or a stack), 9 rows, 9 x 9 and a kernel three planes
     # deep: the tiled kernel, same bar
     rng = np.random.default_rng(sum(shape))
     src = rng.random(shape, dtype=np.float32)

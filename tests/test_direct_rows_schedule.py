@@ -1,15 +1,16 @@
 """The row-strip direct convolution (iane_gb300/csrc/direct_rows.cu) restated in numpy and run on
 the CPU with the kernel's own index arithmetic: TMA boxes of 32 input rows into a 3-slot ring of
 96 rows, box k issued at the start (k < 3) or after step k - 3, waited for and fixed at the end
-of step k - 2 (boxes 0 and 1 before step 0), clamp and mirror fix-ups once per box (the R
+of step k - 2 (boxes 0 and 1 before step 0), clamp and mirror fix-ups once per box (the RX
 columns beside the image by one reflection, then whole rows outside the image from the rows they
 map to), and per lane (4 columns x 8 rows) the window rows base + m with the
 ring's wrap taken as `m < room ? lo : hi`.
 
 Every shared-memory read checks that its slot holds the box the index arithmetic expects and
 that the box has landed (not in flight), every access stays inside the ring, and the whole
-output equals a float64 direct convolution with the border rule -- for K 3, 5 and 7, the three
-borders, ragged image sizes and chunkings, including a last chunk of one row."""
+output equals a float64 direct convolution with the border rule -- for square and non-square
+kernels (line filters included), the three borders, ragged image sizes and chunkings, including a
+last chunk of one row."""
 from __future__ import annotations
 
 import numpy as np
@@ -34,17 +35,17 @@ def map_coord(c, n, border):
 
 def reference(src, k, border):
     ny, nx = src.shape
-    r = k.shape[0] // 2
+    ry, rx = k.shape[0] // 2, k.shape[1] // 2
     out = np.zeros_like(src, dtype=np.float64)
     for y in range(ny):
         for x in range(nx):
             acc = 0.0
             for b in range(k.shape[0]):
-                gy = map_coord(y + r - b, ny, border)
+                gy = map_coord(y + ry - b, ny, border)
                 if gy is None:
                     continue
                 for q in range(k.shape[1]):
-                    gx = map_coord(x + r - q, nx, border)
+                    gx = map_coord(x + rx - q, nx, border)
                     if gx is not None:
                         acc += k[b, q] * src[gy, gx]
             out[y, x] = acc
@@ -55,20 +56,20 @@ class Block:
     def __init__(self, src, k, border, x0, c0, c1):
         self.src, self.k, self.border = src, k, border
         self.ny, self.nx = src.shape
-        self.K = k.shape[0]
-        self.R = self.K // 2
-        self.RA = (self.R + 3) & ~3
-        self.D = self.RA - self.R
+        self.KY, self.KX = k.shape
+        self.RY, self.RX = self.KY // 2, self.KX // 2
+        self.RA = (self.RX + 3) & ~3
+        self.D = self.RA - self.RX
         self.AW = SW + 2 * self.RA
-        self.SEG = (self.D + 4 + 2 * self.R + 3) & ~3
-        self.ROWS = LANE_ROWS + 2 * self.R
+        self.SEG = (self.D + 4 + 2 * self.RX + 3) & ~3
+        self.ROWS = LANE_ROWS + 2 * self.RY
         self.x0, self.c0, self.c1 = x0, c0, c1
-        self.g0 = c0 - self.R
+        self.g0 = c0 - self.RY
         self.ring = np.full((RING, self.AW), np.nan)
         self.slot_box = [None] * SLOTS      # box issued into each slot
         self.landed = [False] * SLOTS
         self.mapped = border != "zero"
-        self.edge_x = self.mapped and (x0 - self.R < 0 or x0 + SW + self.R > self.nx)
+        self.edge_x = self.mapped and (x0 - self.RX < 0 or x0 + SW + self.RX > self.nx)
 
     def issue(self, kb):
         s = kb % SLOTS
@@ -100,13 +101,13 @@ class Block:
 
     def fix(self, kb):
         s = kb % SLOTS
-        R, AW = self.R, self.AW
+        RX, RY, AW = self.RX, self.RY, self.AW
         if self.edge_x:
             clamp = self.border == "clamp"
             for t in range(2 * STEP):           # a thread per row and side, one reflection
                 r, right = t % STEP, t >= STEP
-                for j in range(R):
-                    gx = self.nx + j if right else -R + j
+                for j in range(RX):
+                    gx = self.nx + j if right else -RX + j
                     gm = (self.nx - 1 if clamp else 2 * self.nx - 1 - gx) if right else (0 if clamp else -gx - 1)
                     assert gm == map_coord(gx, self.nx, self.border)
                     c, cs = gx - (self.x0 - self.RA), gm - (self.x0 - self.RA)
@@ -116,7 +117,7 @@ class Block:
         if self.mapped and (top < 0 or top + STEP > self.ny):
             for r in range(STEP):
                 g = top + r
-                if (0 <= g < self.ny) or g < -R or g >= self.ny + R:
+                if (0 <= g < self.ny) or g < -RY or g >= self.ny + RY:
                     continue
                 gm = map_coord(g, self.ny, self.border)
                 src_row = (gm - self.g0) % RING
@@ -137,7 +138,7 @@ class Block:
         self.fix(0)
         self.wait(1)
         self.fix(1)
-        R, K = self.R, self.K
+        RX, RY, KX, KY = self.RX, self.RY, self.KX, self.KY
         for s in range(nsteps):
             for cy in range(4):
                 for cx in range(32):
@@ -154,11 +155,11 @@ class Block:
                         assert lo_col % 4 == 0 and lo_col + self.SEG <= self.AW
                         seg = row[lo_col:lo_col + self.SEG]
                         for j in range(LANE_ROWS):
-                            b = j + 2 * R - m
-                            if 0 <= b < K:
-                                for q in range(K):
+                            b = j + 2 * RY - m
+                            if 0 <= b < KY:
+                                for q in range(KX):
                                     for i in range(4):
-                                        acc[j, i] += self.k[b, q] * seg[self.D + i + 2 * R - q]
+                                        acc[j, i] += self.k[b, q] * seg[self.D + i + 2 * RX - q]
                     x = self.x0 + 4 * cx
                     if x >= self.nx:
                         continue
@@ -186,16 +187,18 @@ def emulate(src, k, border, chunk):
     return dst
 
 
-CASES = [((128, 128), 7, "mirror", 128), ((197, 257), 7, "clamp", 70), ((257, 200), 5, "mirror", 128),
-         ((140, 130), 3, "zero", 40), ((160, 300), 7, "zero", 65), ((258, 131), 7, "mirror", 128),
-         ((129, 256), 5, "clamp", 128)]
+# kernel shapes as (ky, kx)
+CASES = [((128, 128), (7, 7), "mirror", 128), ((197, 257), (7, 7), "clamp", 70), ((257, 200), (5, 5), "mirror", 128),
+         ((140, 130), (3, 3), "zero", 40), ((160, 300), (7, 7), "zero", 65), ((258, 131), (7, 7), "mirror", 128),
+         ((129, 256), (5, 5), "clamp", 128), ((130, 200), (1, 7), "mirror", 128), ((200, 129), (7, 1), "clamp", 70),
+         ((131, 257), (3, 5), "mirror", 64), ((129, 140), (5, 3), "zero", 128), ((160, 130), (1, 3), "clamp", 128)]
 
 
 @pytest.mark.parametrize("shape,k,border,chunk", CASES, ids=[f"{s}-{k}-{b}-{c}" for s, k, b, c in CASES])
 def test_schedule_reads_resident_boxes_and_matches_direct_sums(shape, k, border, chunk):
-    rng = np.random.default_rng(k * 100 + shape[0])
+    rng = np.random.default_rng(k[0] * 100 + k[1] * 10 + shape[0])
     src = rng.random(shape) * 2 - 1
-    taps = rng.random((k, k))
+    taps = rng.random(k)
     got = emulate(src, taps, border, chunk)
     assert not np.isnan(got).any(), "an output was never written"
     np.testing.assert_allclose(got, reference(src, taps, border), rtol=0, atol=1e-12)
